@@ -1,0 +1,380 @@
+// Host half of the C ABI: errors, options, motif generation, the schedule
+// compiler entry point, and decoding schedule tables into a device plan.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "gpm_internal.h"
+#include "graphpi/motif_generator.h"
+#include "graphpi/schedule.h"
+
+namespace gpm {
+
+static thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+Options& options() {
+    static Options o;
+    return o;
+}
+
+namespace {
+
+struct Reader {
+    const int64_t* t;
+    int32_t n, pos = 0;
+    bool ok = true;
+    int64_t get() {
+        if (pos >= n) {
+            ok = false;
+            return 0;
+        }
+        return t[pos++];
+    }
+};
+
+}  // namespace
+
+int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out) {
+    if (!t || n_words <= 0 || !out) {
+        set_error("gpm_plan_create: empty tables");
+        return GPM_ERR_INVALID_ARG;
+    }
+    Reader r{t, n_words};
+    DevPlan p;
+    memset(&p, 0, sizeof p);
+    const int n = (int)r.get();
+    if (n < 2 || n > kMaxN) {
+        set_error("gpm_plan_create: pattern size %d outside 2..%d", n, kMaxN);
+        return GPM_ERR_UNSUPPORTED;
+    }
+    p.n = n;
+    for (int i = 0; i < n * n; ++i) r.get();  // adjacency: not needed by the kernels
+    const int P = (int)r.get();
+    if (P < 1 || P > kMaxPrefix) {
+        set_error("gpm_plan_create: %d prefixes outside 1..%d", P, kMaxPrefix);
+        return GPM_ERR_INVALID_ARG;
+    }
+    p.nprefix = P;
+    int father[kMaxPrefix], last[kMaxN], next[kMaxPrefix];
+    for (int i = 0; i < P; ++i) father[i] = (int)r.get();
+    for (int i = 0; i < n; ++i) last[i] = (int)r.get();
+    for (int i = 0; i < P; ++i) next[i] = (int)r.get();
+    for (int i = 0; i < n; ++i) p.loop_set[i] = (int)r.get();
+    const int R = (int)r.get();
+    if (R < 0 || R > kMaxPrefix) {
+        set_error("gpm_plan_create: %d restrictions outside 0..%d", R, kMaxPrefix);
+        return GPM_ERR_INVALID_ARG;
+    }
+    int rlast[kMaxN], rnext[kMaxPrefix], rindex[kMaxPrefix];
+    for (int i = 0; i < n; ++i) rlast[i] = (int)r.get();
+    for (int i = 0; i < R; ++i) rnext[i] = (int)r.get();
+    for (int i = 0; i < R; ++i) rindex[i] = (int)r.get();
+    const int npairs = (int)r.get();
+    if (npairs < 0 || npairs > 64) {
+        set_error("gpm_plan_create: bad restriction pair count %d", npairs);
+        return GPM_ERR_INVALID_ARG;
+    }
+    for (int i = 0; i < 2 * npairs; ++i) r.get();
+    const int k = (int)r.get();
+    const int ngroups = (int)r.get();
+    if (!r.ok) {
+        set_error("gpm_plan_create: tables truncated");
+        return GPM_ERR_INVALID_ARG;
+    }
+    // --- validate the tree ---
+    for (int i = 0; i < P; ++i) {
+        if (father[i] < -1 || father[i] >= i || next[i] < -1 || next[i] >= P) {
+            set_error("gpm_plan_create: malformed prefix table at %d", i);
+            return GPM_ERR_INVALID_ARG;
+        }
+    }
+    for (int d = 0; d < n; ++d) {
+        if (last[d] < -1 || last[d] >= P || rlast[d] < -1 || rlast[d] >= R) {
+            set_error("gpm_plan_create: malformed depth table at %d", d);
+            return GPM_ERR_INVALID_ARG;
+        }
+        if (d >= 1 && (p.loop_set[d] < 0 || p.loop_set[d] >= P)) {
+            set_error("gpm_plan_create: depth %d has no loop set", d);
+            return GPM_ERR_INVALID_ARG;
+        }
+    }
+    if (k != 0 && (k < 2 || k > n - 1 || k > 6)) {
+        set_error("gpm_plan_create: inclusion-exclusion length %d unsupported", k);
+        return GPM_ERR_UNSUPPORTED;
+    }
+    p.k = k;
+    p.T = k ? n - k : n - 1;
+    p.L = p.T - 1;
+    // chains: prefixes whose last member is depth d, in the reference's order
+    int cnt = 0;
+    for (int d = 0; d < n; ++d) {
+        p.chain_begin[d] = cnt;
+        int guard = 0;
+        for (int id = last[d]; id != -1; id = next[id]) {
+            if (cnt >= kMaxPrefix || ++guard > P) {
+                set_error("gpm_plan_create: cyclic prefix chain at depth %d", d);
+                return GPM_ERR_INVALID_ARG;
+            }
+            p.chain_list[cnt++] = id;
+        }
+    }
+    p.chain_begin[n] = cnt;
+    // restriction masks
+    for (int d = 0; d < n; ++d) {
+        unsigned m = 0;
+        int guard = 0;
+        for (int i = rlast[d]; i != -1; i = rnext[i]) {
+            if (i < 0 || i >= R || ++guard > R) {
+                set_error("gpm_plan_create: malformed restriction list at depth %d", d);
+                return GPM_ERR_INVALID_ARG;
+            }
+            if (rindex[i] < 0 || rindex[i] >= d) {
+                set_error("gpm_plan_create: restriction at depth %d names depth %d", d, rindex[i]);
+                return GPM_ERR_INVALID_ARG;
+            }
+            m |= 1u << rindex[i];
+        }
+        p.rmask[d] = m;
+    }
+    // scratch slots
+    int slots = 0;
+    for (int i = 0; i < P; ++i) {
+        p.father[i] = father[i];
+        p.slot[i] = father[i] >= 0 ? slots++ : -1;
+    }
+    p.nslots = slots + 2;
+    // count-only fusion: without a tail, the prefix built at level L is the
+    // last loop's set and nothing else reads it
+    p.count_only = -1;
+    if (k == 0 && p.L >= 0) {
+        int b = p.chain_begin[p.L], e = p.chain_begin[p.L + 1];
+        if (e - b == 1 && p.chain_list[b] == p.loop_set[p.T] && father[p.chain_list[b]] >= 0)
+            p.count_only = p.chain_list[b];
+    }
+    // inclusion–exclusion groups; singleton blocks get ids 0..k-1
+    p.nblocks = k;
+    for (int i = 0; i < k; ++i) p.block_mask[i] = 1u << i;
+    if (ngroups < 0 || ngroups > kMaxGroups) {
+        set_error("gpm_plan_create: %d inclusion-exclusion groups exceed %d", ngroups, kMaxGroups);
+        return GPM_ERR_UNSUPPORTED;
+    }
+    p.ngroups = ngroups;
+    int entries = 0;
+    for (int g = 0; g < ngroups; ++g) {
+        p.group_coef[g] = (int)r.get();
+        p.group_begin[g] = entries;
+        const int nb = (int)r.get();
+        if (nb < 1 || nb > k) {
+            set_error("gpm_plan_create: malformed inclusion-exclusion group %d", g);
+            return GPM_ERR_INVALID_ARG;
+        }
+        for (int b = 0; b < nb; ++b) {
+            const int len = (int)r.get();
+            if (len < 1 || len > k) {
+                set_error("gpm_plan_create: malformed block in group %d", g);
+                return GPM_ERR_INVALID_ARG;
+            }
+            unsigned mask = 0;
+            for (int j = 0; j < len; ++j) {
+                int m = (int)r.get();
+                if (m < 0 || m >= k) {
+                    set_error("gpm_plan_create: block member %d out of range", m);
+                    return GPM_ERR_INVALID_ARG;
+                }
+                mask |= 1u << m;
+            }
+            int id = -1;
+            for (int q = 0; q < p.nblocks; ++q)
+                if (p.block_mask[q] == mask) id = q;
+            if (id < 0) {
+                if (p.nblocks >= kMaxBlocks) {
+                    set_error("gpm_plan_create: too many inclusion-exclusion blocks");
+                    return GPM_ERR_UNSUPPORTED;
+                }
+                id = p.nblocks++;
+                p.block_mask[id] = mask;
+            }
+            if (entries >= kMaxGroupEntries) {
+                set_error("gpm_plan_create: inclusion-exclusion table too large");
+                return GPM_ERR_UNSUPPORTED;
+            }
+            p.group_block[entries++] = (unsigned char)id;
+        }
+    }
+    p.group_begin[ngroups] = entries;
+    p.redundancy = r.get();
+    if (!r.ok || p.redundancy < 1) {
+        set_error("gpm_plan_create: tables truncated or redundancy < 1");
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (k && ngroups == 0) {
+        set_error("gpm_plan_create: inclusion-exclusion length %d without groups", k);
+        return GPM_ERR_INVALID_ARG;
+    }
+    *out = p;
+    return GPM_OK;
+}
+
+}  // namespace gpm
+
+using gpm::set_error;
+
+extern "C" {
+
+GPM_API const char* gpm_last_error(void) { return gpm::g_last_error.c_str(); }
+
+GPM_API int gpm_motifs(int32_t k, int32_t* adj_out, int32_t cap, int32_t* count) {
+    gpm::clear_error();
+    if (k < 1 || k > gpm::kMaxN || !count || (cap > 0 && !adj_out)) {
+        set_error("gpm_motifs: k must be in 1..%d", gpm::kMaxN);
+        return GPM_ERR_INVALID_ARG;
+    }
+    MotifGenerator mg(k);
+    std::vector<Pattern> ps = mg.generate();
+    int c = 0;
+    for (const Pattern& p : ps) {
+        if (c < cap) memcpy(adj_out + (size_t)c * k * k, p.get_adj_mat_ptr(), sizeof(int32_t) * k * k);
+        ++c;
+    }
+    *count = c;
+    return GPM_OK;
+}
+
+GPM_API int gpm_pattern_multiplicity(int32_t n, const int32_t* adj, int64_t* out) {
+    gpm::clear_error();
+    if (n < 1 || n > gpm::kMaxN || !adj || !out) {
+        set_error("gpm_pattern_multiplicity: bad arguments");
+        return GPM_ERR_INVALID_ARG;
+    }
+    Pattern p(n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            if (adj[i * n + j]) p.add_edge(i, j);
+    // multiplicity is a property of the matrix; any loop order will do
+    int64_t m = 0;
+    {
+        std::vector<int> perm(n);
+        for (int i = 0; i < n; ++i) perm[i] = i;
+        do {
+            bool ok = true;
+            for (int i = 0; i < n && ok; ++i)
+                for (int j = i + 1; j < n; ++j)
+                    if (p.get_adj_mat_ptr()[i * n + j] && !p.get_adj_mat_ptr()[perm[i] * n + perm[j]]) {
+                        ok = false;
+                        break;
+                    }
+            m += ok;
+        } while (std::next_permutation(perm.begin(), perm.end()));
+    }
+    *out = m;
+    return GPM_OK;
+}
+
+GPM_API int gpm_schedule_build(int32_t n, const int32_t* adj, int32_t perf_type, int32_t restricts_type,
+                               int32_t use_iep, int64_t v_cnt, uint64_t e_cnt, int64_t tri_cnt, int64_t* tables,
+                               int32_t cap, int32_t* n_words, int32_t* valid) {
+    gpm::clear_error();
+    if (n < 2 || n > gpm::kMaxN || !adj || !n_words || !valid) {
+        set_error("gpm_schedule_build: pattern size must be in 2..%d", gpm::kMaxN);
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (perf_type < 0 || perf_type > 3 || restricts_type < 0 || restricts_type > 2) {
+        set_error("gpm_schedule_build: perf_type must be 0..3 and restricts_type 0..2");
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (perf_type != 0 && tri_cnt < 0) {
+        set_error("gpm_schedule_build: performance modeling needs tri_cnt >= 0");
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (v_cnt < 1 || v_cnt > INT32_MAX || e_cnt > UINT32_MAX || (perf_type != 0 && e_cnt == 0)) {
+        set_error("gpm_schedule_build: v_cnt/e_cnt out of range");
+        return GPM_ERR_INVALID_ARG;
+    }
+    try {
+        Pattern p(n);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                if (adj[i * n + j] != adj[j * n + i]) {
+                    set_error("gpm_schedule_build: adjacency matrix is not symmetric");
+                    return GPM_ERR_INVALID_ARG;
+                }
+                if (adj[i * n + j] && i != j) p.add_edge(i, j);
+            }
+        bool ok = false;
+        Schedule s(p, ok, perf_type, restricts_type, use_iep != 0, (int)v_cnt, (unsigned)e_cnt, tri_cnt);
+        *valid = ok ? 1 : 0;
+        std::vector<int64_t> t = ok ? s.pack() : std::vector<int64_t>();
+        *n_words = (int32_t)t.size();
+        if ((int32_t)t.size() > cap || (!tables && !t.empty())) {
+            set_error("gpm_schedule_build: output needs %d words, capacity %d", (int)t.size(), cap);
+            return GPM_ERR_INVALID_ARG;
+        }
+        if (!t.empty()) memcpy(tables, t.data(), t.size() * sizeof(int64_t));
+        return GPM_OK;
+    } catch (const std::exception& e) {
+        set_error("gpm_schedule_build: %s", e.what());
+        return GPM_ERR_INVALID_ARG;
+    }
+}
+
+GPM_API int gpm_set_option(const char* key, int64_t value) {
+    gpm::clear_error();
+    if (!key) return GPM_ERR_INVALID_ARG;
+    gpm::Options& o = gpm::options();
+    std::string k(key);
+    int64_t* slot = nullptr;
+    int64_t lo = 0, hi = INT64_MAX;
+    if (k == "warps_per_block") slot = &o.warps_per_block, lo = 1, hi = 32;
+    else if (k == "blocks_per_sm") slot = &o.blocks_per_sm, lo = 1, hi = 32;
+    else if (k == "chunk") slot = &o.chunk, lo = 1, hi = 1 << 20;
+    else if (k == "count_bytes") slot = &o.count_bytes, lo = 0, hi = 1;
+    else if (k == "timeout_ms") slot = &o.timeout_ms, lo = 1, hi = 3600 * 1000;
+    else if (k == "stage_max") slot = &o.stage_max, lo = 0, hi = 1 << 16;
+    else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
+    if (!slot) {
+        set_error("gpm_set_option: unknown key '%s'", key);
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (value < lo || value > hi) {
+        set_error("gpm_set_option: %s=%lld outside [%lld, %lld]", key, (long long)value, (long long)lo, (long long)hi);
+        return GPM_ERR_INVALID_ARG;
+    }
+    *slot = value;
+    return GPM_OK;
+}
+
+GPM_API int gpm_get_option(const char* key, int64_t* value) {
+    gpm::clear_error();
+    if (!key || !value) return GPM_ERR_INVALID_ARG;
+    gpm::Options& o = gpm::options();
+    std::string k(key);
+    if (k == "warps_per_block") *value = o.warps_per_block;
+    else if (k == "blocks_per_sm") *value = o.blocks_per_sm;
+    else if (k == "chunk") *value = o.chunk;
+    else if (k == "count_bytes") *value = o.count_bytes;
+    else if (k == "timeout_ms") *value = o.timeout_ms;
+    else if (k == "stage_max") *value = o.stage_max;
+    else if (k == "split") *value = o.split;
+    else {
+        set_error("gpm_get_option: unknown key '%s'", key);
+        return GPM_ERR_INVALID_ARG;
+    }
+    return GPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,1024 @@
+// GB300 (sm_103a) kernels and the device half of the C ABI.
+//
+// The hot path is the schedule-driven nested-loop enumeration of
+// Graph::pattern_matching / pattern_matching_aggressive_func
+// (reference src/graph.cpp:199-398), re-planned for the GPU:
+//   * persistent warps pull first-level edges (v0, v1) — or root vertices
+//     when the tail starts at depth 1 — from per-(pattern, graph) atomic
+//     work queues; a chunk of consecutive edges shares v0;
+//   * every prefix set (VertexSet::build_vertex_set, src/vertex_set.cpp:158)
+//     is built by a warp-cooperative intersection: lanes take 32 elements of
+//     the smaller sorted list, binary-search the larger one from a moving
+//     lower bound, and compact hits with __ballot_sync/__popc;
+//   * the last loop's set is never written out: its size below the
+//     restriction bound and minus the chosen vertices is counted during the
+//     intersection (src/graph.cpp:346-364 fused with :383-390);
+//   * the inclusion–exclusion tail (src/graph.cpp:306-344) evaluates each
+//     distinct block once and combines groups in 128-bit integers;
+//   * per-warp sums are 128-bit and reach the per-pair result through two
+//     64-bit atomics with carry, so counts above 2^64 stay exact.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include <cub/cub.cuh>
+
+#include "gpm_internal.h"
+
+namespace gpm {
+
+#define GPM_CK(call)                                                                               \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) {                                                                   \
+            set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? GPM_ERR_OOM : GPM_ERR_CUDA;                  \
+        }                                                                                          \
+    } while (0)
+
+constexpr unsigned kFull = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// device building blocks
+
+struct GraphView {
+    const unsigned* __restrict__ rowptr;
+    const int* __restrict__ col;
+    int v_cnt;
+    int pad_;
+    unsigned long long e_cnt;
+};
+
+struct PairDesc {
+    GraphView g;
+    const DevPlan* plan;
+    unsigned long long ntasks;  // v_cnt when the tail starts at depth 1, else e_cnt
+    int cap;                    // scratch ints per slot for this graph
+    int pad_;
+};
+
+struct WarpState {
+    int chosen[kMaxN];
+    int idx[kMaxN];
+    int end[kMaxN];
+    int len[kMaxPrefix];
+    const int* ptr[kMaxPrefix];
+    const int* lp[kMaxN];
+    int blockval[kMaxBlocks];
+};
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// first index i in a[0, n) with a[i] >= x (all lanes search the same key)
+__device__ __forceinline__ int lower_bound_u(const int* __restrict__ a, int n, int x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// A ∩ B written sorted to out; returns its size.
+__device__ int isect_store(const int* __restrict__ A, int na, const int* __restrict__ B, int nb,
+                           int* __restrict__ out, int lane) {
+    if (na > nb) {
+        const int* t = A; A = B; B = t;
+        int u = na; na = nb; nb = u;
+    }
+    int written = 0, lo = 0;
+    for (int base = 0; base < na; base += 32) {
+        const int i = base + lane;
+        const bool valid = i < na;
+        const int x = valid ? A[i] : INT_MAX;
+        int l = lo, h = nb;
+        while (l < h) {
+            int m = (l + h) >> 1;
+            if (B[m] < x) l = m + 1;
+            else h = m;
+        }
+        const bool found = valid && l < nb && B[l] == x;
+        const unsigned mask = __ballot_sync(kFull, found);
+        if (found) out[written + __popc(mask & lanemask_lt())] = x;
+        written += __popc(mask);
+        lo = __shfl_sync(kFull, l, 31);
+    }
+    __syncwarp();
+    return written;
+}
+
+// |A ∩ B ∩ [0, bound) \ chosen[0, nch)|
+__device__ int isect_count(const int* __restrict__ A, int na, const int* __restrict__ B, int nb, int bound,
+                           const int* chosen, int nch, int lane) {
+    na = lower_bound_u(A, na, bound);
+    nb = lower_bound_u(B, nb, bound);
+    if (na > nb) {
+        const int* t = A; A = B; B = t;
+        int u = na; na = nb; nb = u;
+    }
+    int cnt = 0, lo = 0;
+    for (int base = 0; base < na; base += 32) {
+        const int i = base + lane;
+        const bool valid = i < na;
+        const int x = valid ? A[i] : INT_MAX;
+        int l = lo, h = nb;
+        while (l < h) {
+            int m = (l + h) >> 1;
+            if (B[m] < x) l = m + 1;
+            else h = m;
+        }
+        bool found = valid && l < nb && B[l] == x;
+        if (found)
+            for (int j = 0; j < nch; ++j)
+                if (chosen[j] == x) found = false;
+        cnt += __popc(__ballot_sync(kFull, found));
+        lo = __shfl_sync(kFull, l, 31);
+    }
+    return cnt;
+}
+
+// |S[0, len) \ chosen[0, nch)|  (VertexSet::unorderd_subtraction_size,
+// src/vertex_set.cpp:196-209)
+__device__ __forceinline__ int count_outside(const int* __restrict__ S, int len, const int* chosen, int nch, int lane) {
+    bool in = false;
+    if (lane < nch) {
+        const int c = chosen[lane];
+        const int p = lower_bound_u(S, len, c);
+        in = p < len && S[p] == c;
+    }
+    return len - __popc(__ballot_sync(kFull, in));
+}
+
+__device__ __forceinline__ void add128(unsigned long long* o, __int128 v) {
+    const unsigned long long lo = (unsigned long long)v;
+    const unsigned long long hi = (unsigned long long)(v >> 64);
+    const unsigned long long old = atomicAdd(o, lo);
+    const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
+    if (hi + carry) atomicAdd(o + 1, hi + carry);
+}
+
+template <bool kBytes>
+struct WarpCtx {
+    WarpState* s;
+    const DevPlan* __restrict__ P;
+    GraphView g;
+    int* scratch;
+    int cap;
+    int lane;
+    unsigned long long bytes;
+
+    __device__ __forceinline__ void nbr(int v, const int*& p, int& d) const {
+        const unsigned a = g.rowptr[v], b = g.rowptr[v + 1];
+        p = g.col + a;
+        d = (int)(b - a);
+    }
+
+    __device__ __forceinline__ int bound_of(int d) const {
+        unsigned m = P->rmask[d];
+        int b = g.v_cnt;
+        while (m) {
+            const int j = __ffs(m) - 1;
+            m &= m - 1;
+            b = min(b, s->chosen[j]);
+        }
+        return b;
+    }
+
+    __device__ __forceinline__ bool in_chosen(int v, int d) const {
+        bool hit = false;
+        for (int j = 0; j < d; ++j) hit |= s->chosen[j] == v;
+        return hit;
+    }
+
+    __device__ __forceinline__ void set_chosen(int d, int v) {
+        if (lane == 0) s->chosen[d] = v;
+        __syncwarp();
+    }
+
+    // Builds the prefix sets whose last member is depth d for candidate v.
+    __device__ bool build_chain(int d, const int* nv, int dv) {
+        const int b = P->chain_begin[d], e = P->chain_begin[d + 1];
+        for (int c = b; c < e; ++c) {
+            const int pid = P->chain_list[c];
+            const int f = P->father[pid];
+            const int* ptr;
+            int len;
+            if (f < 0) {
+                ptr = nv;
+                len = dv;
+            } else {
+                int* dst = scratch + (size_t)P->slot[pid] * cap;
+                const int lf = s->len[f];
+                len = isect_store(s->ptr[f], lf, nv, dv, dst, lane);
+                ptr = dst;
+                if (kBytes) bytes += 4ull * (unsigned long long)(lf + dv);
+            }
+            if (lane == 0) {
+                s->ptr[pid] = ptr;
+                s->len[pid] = len;
+            }
+            __syncwarp();
+            if (len == 0) return false;
+        }
+        return true;
+    }
+
+    // inclusion–exclusion tail at depth T (src/graph.cpp:306-344)
+    __device__ __int128 iep_tail() {
+        const int T = P->T, k = P->k;
+        for (int i = 0; i < k; ++i) {
+            const int sid = P->loop_set[T + i];
+            const int v = count_outside(s->ptr[sid], s->len[sid], s->chosen, T, lane);
+            if (v == 0) return 0;  // every group holds a block inside S_i
+            if (lane == 0) s->blockval[i] = v;
+        }
+        const int tmp0 = P->nslots - 2;
+        for (int b = k; b < P->nblocks; ++b) {
+            unsigned m = P->block_mask[b];
+            int j = __ffs(m) - 1;
+            m &= m - 1;
+            const int* A = s->ptr[P->loop_set[T + j]];
+            int na = s->len[P->loop_set[T + j]];
+            int flip = 0;
+            while (__popc(m) > 1 && na > 0) {
+                j = __ffs(m) - 1;
+                m &= m - 1;
+                const int sid = P->loop_set[T + j];
+                int* dst = scratch + (size_t)(tmp0 + flip) * cap;
+                if (kBytes) bytes += 4ull * (unsigned long long)(na + s->len[sid]);
+                na = isect_store(A, na, s->ptr[sid], s->len[sid], dst, lane);
+                A = dst;
+                flip ^= 1;
+            }
+            int val = 0;
+            if (na > 0) {
+                j = __ffs(m) - 1;
+                const int sid = P->loop_set[T + j];
+                if (kBytes) bytes += 4ull * (unsigned long long)(na + s->len[sid]);
+                val = isect_count(A, na, s->ptr[sid], s->len[sid], INT_MAX, s->chosen, T, lane);
+            }
+            if (lane == 0) s->blockval[b] = val;
+        }
+        __syncwarp();
+        __int128 total = 0;
+        if (lane == 0) {
+            for (int g2 = 0; g2 < P->ngroups; ++g2) {
+                __int128 v = P->group_coef[g2];
+                for (int q = P->group_begin[g2]; q < P->group_begin[g2 + 1]; ++q) {
+                    v *= (__int128)s->blockval[P->group_block[q]];
+                    if (v == 0) break;
+                }
+                total += v;
+            }
+        }
+        return total;
+    }
+
+    // the reference's work at depth T once chosen[0, T) and all sets exist
+    __device__ __int128 tail_at_T() {
+        const int T = P->T;
+        const int sid = P->loop_set[T];
+        const int len = s->len[sid];
+        if (len <= 0) return 0;
+        if (P->k) return iep_tail();
+        const int* S = s->ptr[sid];
+        const int lb = lower_bound_u(S, len, bound_of(T));
+        return (__int128)count_outside(S, lb, s->chosen, T, lane);
+    }
+
+    // candidate v at the deepest loop level L
+    __device__ __int128 tail_with_candidate(int v, const int* nv, int dv) {
+        const int L = P->L;
+        if (P->count_only >= 0) {
+            set_chosen(L, v);
+            const int f = P->father[P->count_only];
+            if (kBytes) bytes += 4ull * (unsigned long long)(s->len[f] + dv);
+            return (__int128)isect_count(s->ptr[f], s->len[f], nv, dv, bound_of(P->T), s->chosen, P->T, lane);
+        }
+        if (!build_chain(L, nv, dv)) return 0;
+        set_chosen(L, v);
+        return tail_at_T();
+    }
+
+    __device__ void start_level(int d) {
+        const int sid = P->loop_set[d];
+        const int* S = s->ptr[sid];
+        const int e = lower_bound_u(S, s->len[sid], bound_of(d));
+        if (lane == 0) {
+            s->lp[d] = S;
+            s->idx[d] = 0;
+            s->end[d] = e;
+        }
+        __syncwarp();
+    }
+
+    // levels 2..L below a fixed (v0, v1)
+    __device__ __int128 dfs_from_2() {
+        const int L = P->L;
+        __int128 acc = 0;
+        int d = 2;
+        start_level(2);
+        while (d >= 2) {
+            const int i = s->idx[d];
+            if (i >= s->end[d]) {
+                --d;
+                continue;
+            }
+            const int v = s->lp[d][i];
+            __syncwarp();
+            if (lane == 0) s->idx[d] = i + 1;
+            __syncwarp();
+            if (in_chosen(v, d)) continue;
+            const int* nv;
+            int dv;
+            nbr(v, nv, dv);
+            if (kBytes) bytes += 8;
+            if (d == L) {
+                acc += tail_with_candidate(v, nv, dv);
+                continue;
+            }
+            if (!build_chain(d, nv, dv)) continue;
+            set_chosen(d, v);
+            ++d;
+            start_level(d);
+        }
+        return acc;
+    }
+
+    __device__ __int128 edge_task(int v0, int v1) {
+        if ((P->rmask[1] & 1u) && v1 >= v0) return 0;
+        const int* n0;
+        int d0;
+        nbr(v0, n0, d0);
+        set_chosen(0, v0);
+        if (!build_chain(0, n0, d0)) return 0;
+        const int* n1;
+        int d1;
+        nbr(v1, n1, d1);
+        if (kBytes) bytes += 16;
+        if (P->L == 1) return tail_with_candidate(v1, n1, d1);
+        if (!build_chain(1, n1, d1)) return 0;
+        set_chosen(1, v1);
+        return dfs_from_2();
+    }
+
+    __device__ __int128 root_task(int v0) {
+        const int* n0;
+        int d0;
+        nbr(v0, n0, d0);
+        if (kBytes) bytes += 8;
+        set_chosen(0, v0);
+        if (!build_chain(0, n0, d0)) return 0;
+        return tail_at_T();
+    }
+};
+
+template <bool kBytes>
+__global__ void __launch_bounds__(256) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
+                                                    unsigned long long* __restrict__ cursors,
+                                                    unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
+                                                    long long scratch_per_warp, int chunk,
+                                                    unsigned long long* __restrict__ stats) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    WarpCtx<kBytes> w;
+    w.s = reinterpret_cast<WarpState*>(smem_raw) + wid;
+    w.scratch = scratch_all + gw * scratch_per_warp;
+    w.lane = lane;
+    w.bytes = 0;
+    for (int p = 0; p < npairs; ++p) {
+        const PairDesc pd = pairs[p];
+        w.P = pd.plan;
+        w.g = pd.g;
+        w.cap = pd.cap;
+        const int T = w.P->T;
+        __int128 acc = 0;
+        int cur_v0 = -1;
+        unsigned cur_lo = 0, cur_hi = 0;
+        for (;;) {
+            unsigned long long t0 = 0;
+            if (lane == 0) t0 = atomicAdd(&cursors[p], (unsigned long long)chunk);
+            t0 = __shfl_sync(kFull, t0, 0);
+            if (t0 >= pd.ntasks) break;
+            const unsigned long long t1 = min(t0 + (unsigned long long)chunk, pd.ntasks);
+            for (unsigned long long t = t0; t < t1; ++t) {
+                if (T == 1) {
+                    acc += w.root_task((int)t);
+                    continue;
+                }
+                const unsigned e = (unsigned)t;
+                if (cur_v0 < 0 || e < cur_lo || e >= cur_hi) {
+                    // last v with rowptr[v] <= e
+                    int lo = 0, hi = pd.g.v_cnt;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (pd.g.rowptr[mid] <= e) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    cur_v0 = lo;
+                    cur_lo = pd.g.rowptr[lo];
+                    cur_hi = pd.g.rowptr[lo + 1];
+                }
+                acc += w.edge_task(cur_v0, pd.g.col[e]);
+            }
+        }
+        if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
+    }
+    if (kBytes && lane == 0 && w.bytes) atomicAdd(stats, w.bytes);
+}
+
+// Triangle count: sum over v, u in N(v) with u < v of |N(v) ∩ N(u) ∩ [0, u)|
+// (Graph::tc_mt / intersection_size_clique, src/graph.cpp:66-95,121-139).
+__global__ void __launch_bounds__(256) tc_kernel(GraphView g, unsigned long long* __restrict__ cursor,
+                                                 unsigned long long* __restrict__ out, int chunk) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long acc = 0;
+    int cur_v = -1;
+    unsigned cur_lo = 0, cur_hi = 0;
+    for (;;) {
+        unsigned long long t0 = 0;
+        if (lane == 0) t0 = atomicAdd(cursor, (unsigned long long)chunk);
+        t0 = __shfl_sync(kFull, t0, 0);
+        if (t0 >= g.e_cnt) break;
+        const unsigned long long t1 = min(t0 + (unsigned long long)chunk, g.e_cnt);
+        for (unsigned long long t = t0; t < t1; ++t) {
+            const unsigned e = (unsigned)t;
+            if (cur_v < 0 || e < cur_lo || e >= cur_hi) {
+                int lo = 0, hi = g.v_cnt;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (g.rowptr[mid] <= e) lo = mid;
+                    else hi = mid - 1;
+                }
+                cur_v = lo;
+                cur_lo = g.rowptr[lo];
+                cur_hi = g.rowptr[lo + 1];
+            }
+            const int u = g.col[e];
+            if (u >= cur_v) continue;
+            const unsigned ub = g.rowptr[u], ue = g.rowptr[u + 1];
+            acc += (unsigned long long)isect_count(g.col + cur_lo, (int)(cur_hi - cur_lo), g.col + ub, (int)(ue - ub), u,
+                                                   nullptr, 0, lane);
+        }
+    }
+    if (lane == 0 && acc) atomicAdd(out, acc);
+}
+
+// CSR checks: offsets monotone, ids in range, rows strictly increasing, no
+// self loops, every edge present in both directions.
+__global__ void validate_kernel(GraphView g, unsigned* __restrict__ flags) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    unsigned bad = 0;
+    for (long long v = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < g.v_cnt; v += warps) {
+        const unsigned a = g.rowptr[v], b = g.rowptr[v + 1];
+        if (b < a || b > g.e_cnt) {
+            bad |= 1;
+            continue;
+        }
+        for (unsigned k = a + lane; k < b; k += 32) {
+            const int x = g.col[k];
+            if (x < 0 || x >= g.v_cnt) {
+                bad |= 2;
+                continue;
+            }
+            if (x == (int)v) bad |= 4;
+            if (k > a && g.col[k - 1] >= x) bad |= 8;
+            const unsigned xa = g.rowptr[x], xb = g.rowptr[x + 1];
+            if (xb < xa || xb > g.e_cnt) {
+                bad |= 1;
+                continue;
+            }
+            const int p = lower_bound_u(g.col + xa, (int)(xb - xa), (int)v);
+            if (p >= (int)(xb - xa) || g.col[xa + p] != (int)v) bad |= 16;
+        }
+    }
+    if (bad) atomicOr(flags, bad);
+}
+
+__global__ void degree_keys_kernel(const unsigned* __restrict__ rowptr, int v_cnt, unsigned* __restrict__ keys,
+                                   int* __restrict__ ids) {
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < v_cnt; v += (long long)gridDim.x * blockDim.x) {
+        keys[v] = ~(rowptr[v + 1] - rowptr[v]);  // descending degree
+        ids[v] = (int)v;
+    }
+}
+
+__global__ void relabel_maps_kernel(const unsigned* __restrict__ rowptr, const int* __restrict__ order, int v_cnt,
+                                    int* __restrict__ new_id, unsigned* __restrict__ new_deg) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i <= v_cnt; i += (long long)gridDim.x * blockDim.x) {
+        if (i == v_cnt) {
+            new_deg[i] = 0;
+            continue;
+        }
+        const int o = order[i];
+        new_id[o] = (int)i;
+        new_deg[i] = rowptr[o + 1] - rowptr[o];
+    }
+}
+
+__global__ void relabel_fill_kernel(const unsigned* __restrict__ rowptr, const int* __restrict__ col,
+                                    const int* __restrict__ order, const int* __restrict__ new_id,
+                                    const unsigned* __restrict__ new_rowptr, int v_cnt, int* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < v_cnt; i += warps) {
+        const int o = order[i];
+        const unsigned a = rowptr[o], b = rowptr[o + 1], dst = new_rowptr[i];
+        for (unsigned k = a + lane; k < b; k += 32) out[dst + (k - a)] = new_id[col[k]];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct DeviceCtx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    std::mutex mu;
+};
+
+static thread_local int t_device = 0;
+static thread_local double t_ms = 0;
+static thread_local int64_t t_launches = 0;
+static thread_local uint64_t t_bytes = 0;
+
+static DeviceCtx* get_ctx(int* err) {
+    static std::mutex mu;
+    static DeviceCtx* ctxs[64] = {nullptr};
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        set_error("no CUDA device available (%s)", e == cudaSuccess ? "0 devices" : cudaGetErrorString(e));
+        *err = GPM_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    if (t_device < 0 || t_device >= n || t_device >= 64) {
+        set_error("device %d not present", t_device);
+        *err = GPM_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    DeviceCtx*& c = ctxs[t_device];
+    if (!c) {
+        DeviceCtx* nc = new DeviceCtx();
+        nc->device = t_device;
+        if (cudaSetDevice(t_device) != cudaSuccess ||
+            cudaDeviceGetAttribute(&nc->num_sms, cudaDevAttrMultiProcessorCount, t_device) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&nc->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&nc->ev0) != cudaSuccess || cudaEventCreate(&nc->ev1) != cudaSuccess) {
+            set_error("CUDA initialisation failed on device %d: %s", t_device, cudaGetErrorString(cudaGetLastError()));
+            delete nc;
+            *err = GPM_ERR_CUDA;
+            return nullptr;
+        }
+        c = nc;
+    }
+    if (cudaSetDevice(t_device) != cudaSuccess) {
+        set_error("cudaSetDevice(%d) failed", t_device);
+        *err = GPM_ERR_CUDA;
+        return nullptr;
+    }
+    *err = GPM_OK;
+    return c;
+}
+
+static int ensure_scratch(DeviceCtx* c, size_t bytes) {
+    if (c->scratch_bytes >= bytes) return GPM_OK;
+    if (c->scratch) cudaFree(c->scratch);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+    GPM_CK(cudaMalloc(&c->scratch, bytes));
+    c->scratch_bytes = bytes;
+    return GPM_OK;
+}
+
+// RAII device buffer for one call
+struct DevBuf {
+    void* p = nullptr;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
+    const int V = g->v_cnt;
+    const unsigned E = (unsigned)g->e_cnt;
+    cudaStream_t st = c->stream;
+    DevBuf keys, keys2, ids, order, tmp;
+    GPM_CK(cudaMalloc(&keys.p, sizeof(unsigned) * (size_t)std::max(V, 1)));
+    GPM_CK(cudaMalloc(&keys2.p, sizeof(unsigned) * (size_t)std::max(V, 1)));
+    GPM_CK(cudaMalloc(&ids.p, sizeof(int) * (size_t)std::max(V, 1)));
+    GPM_CK(cudaMalloc(&order.p, sizeof(int) * (size_t)std::max(V, 1)));
+    const int threads = 256, blocks = c->num_sms * 8;
+    degree_keys_kernel<<<blocks, threads, 0, st>>>(g->rowptr, V, (unsigned*)keys.p, (int*)ids.p);
+    GPM_CK(cudaGetLastError());
+    size_t tb = 0;
+    GPM_CK(cub::DeviceRadixSort::SortPairs(nullptr, tb, (unsigned*)keys.p, (unsigned*)keys2.p, (int*)ids.p,
+                                           (int*)order.p, V, 0, 32, st));
+    GPM_CK(cudaMalloc(&tmp.p, std::max<size_t>(tb, 1)));
+    GPM_CK(cub::DeviceRadixSort::SortPairs(tmp.p, tb, (unsigned*)keys.p, (unsigned*)keys2.p, (int*)ids.p,
+                                           (int*)order.p, V, 0, 32, st));
+    unsigned top[2] = {~0u, ~0u};
+    GPM_CK(cudaMemcpyAsync(top, keys2.p, sizeof(unsigned) * std::min(V, 2), cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    g->max_degree = V >= 1 ? (int)~top[0] : 0;
+    g->max_isect = V >= 2 ? (int)~top[1] : g->max_degree;
+    if (!relabel || V == 0 || E == 0) return GPM_OK;
+
+    DevBuf new_id, new_deg, new_rowptr, new_col_u, new_col, tmp2;
+    GPM_CK(cudaMalloc(&new_id.p, sizeof(int) * (size_t)V));
+    GPM_CK(cudaMalloc(&new_deg.p, sizeof(unsigned) * ((size_t)V + 1)));
+    GPM_CK(cudaMalloc(&new_rowptr.p, sizeof(unsigned) * ((size_t)V + 1)));
+    GPM_CK(cudaMalloc(&new_col_u.p, sizeof(int) * (size_t)E));
+    GPM_CK(cudaMalloc(&new_col.p, sizeof(int) * (size_t)E));
+    relabel_maps_kernel<<<blocks, threads, 0, st>>>(g->rowptr, (const int*)order.p, V, (int*)new_id.p,
+                                                    (unsigned*)new_deg.p);
+    GPM_CK(cudaGetLastError());
+    size_t sb = 0;
+    GPM_CK(cub::DeviceScan::ExclusiveSum(nullptr, sb, (unsigned*)new_deg.p, (unsigned*)new_rowptr.p, V + 1, st));
+    GPM_CK(cudaMalloc(&tmp2.p, std::max<size_t>(sb, 1)));
+    GPM_CK(cub::DeviceScan::ExclusiveSum(tmp2.p, sb, (unsigned*)new_deg.p, (unsigned*)new_rowptr.p, V + 1, st));
+    relabel_fill_kernel<<<blocks, threads, 0, st>>>(g->rowptr, g->col, (const int*)order.p, (const int*)new_id.p,
+                                                    (const unsigned*)new_rowptr.p, V, (int*)new_col_u.p);
+    GPM_CK(cudaGetLastError());
+    size_t ssb = 0;
+    GPM_CK(cub::DeviceSegmentedSort::SortKeys(nullptr, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
+                                              (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
+    DevBuf tmp3;
+    GPM_CK(cudaMalloc(&tmp3.p, std::max<size_t>(ssb, 1)));
+    GPM_CK(cub::DeviceSegmentedSort::SortKeys(tmp3.p, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
+                                              (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    cudaFree(g->rowptr);
+    cudaFree(g->col);
+    g->rowptr = (uint32_t*)new_rowptr.p;
+    new_rowptr.p = nullptr;
+    g->col = (int32_t*)new_col.p;
+    new_col.p = nullptr;
+    g->relabelled = true;
+    return GPM_OK;
+}
+
+static GraphView view_of(const gpm_graph* g) {
+    GraphView v;
+    v.rowptr = g->rowptr;
+    v.col = g->col;
+    v.v_cnt = g->v_cnt;
+    v.pad_ = 0;
+    v.e_cnt = g->e_cnt;
+    return v;
+}
+
+// Launches the matcher over n pairs and leaves raw 128-bit sums in host_raw
+// (2 words per pair).
+static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_plan* const* plans,
+                     unsigned long long* host_raw) {
+    Options& o = options();
+    int cap = 1, nslots = 1;
+    std::vector<PairDesc> descs(n);
+    for (int i = 0; i < n; ++i) {
+        const gpm_graph* g = graphs[i];
+        const gpm_plan* p = plans[i];
+        if (!g || !p) {
+            set_error("pair %d: null graph or plan", i);
+            return GPM_ERR_INVALID_ARG;
+        }
+        if (g->device != c->device || p->device != c->device) {
+            set_error("pair %d: graph/plan live on another device", i);
+            return GPM_ERR_INVALID_ARG;
+        }
+        descs[i].g = view_of(g);
+        descs[i].plan = p->dev;
+        descs[i].ntasks = p->host.T == 1 ? (unsigned long long)g->v_cnt : (unsigned long long)g->e_cnt;
+        descs[i].cap = std::max(1, g->max_isect);
+        descs[i].pad_ = 0;
+        cap = std::max(cap, descs[i].cap);
+        nslots = std::max(nslots, p->host.nslots);
+    }
+    const int wpb = (int)o.warps_per_block;
+    long long blocks = (long long)c->num_sms * o.blocks_per_sm;
+    const long long per_warp = (long long)nslots * cap;
+    // shrink the grid when the per-warp scratch would not fit in free memory
+    size_t free_b = 0, total_b = 0;
+    GPM_CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = (size_t)((free_b + c->scratch_bytes) * 0.6);
+    while (blocks > 1 && (size_t)blocks * wpb * per_warp * sizeof(int) > budget) blocks = (blocks + 1) / 2;
+    int rc = ensure_scratch(c, (size_t)blocks * wpb * per_warp * sizeof(int));
+    if (rc) return rc;
+    DevBuf d_pairs, d_small;
+    GPM_CK(cudaMalloc(&d_pairs.p, sizeof(PairDesc) * n));
+    const size_t small_words = (size_t)n + 2 * (size_t)n + 2;  // cursors, out, stats
+    GPM_CK(cudaMalloc(&d_small.p, small_words * sizeof(unsigned long long)));
+    unsigned long long* cursors = (unsigned long long*)d_small.p;
+    unsigned long long* out = cursors + n;
+    unsigned long long* stats = out + 2 * n;
+    cudaStream_t st = c->stream;
+    GPM_CK(cudaMemcpyAsync(d_pairs.p, descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
+    GPM_CK(cudaMemsetAsync(d_small.p, 0, small_words * sizeof(unsigned long long), st));
+    const size_t smem = sizeof(WarpState) * wpb;
+    GPM_CK(cudaEventRecord(c->ev0, st));
+    if (o.count_bytes)
+        match_kernel<true><<<(unsigned)blocks, wpb * 32, smem, st>>>((const PairDesc*)d_pairs.p, n, cursors, out,
+                                                                     (int*)c->scratch, per_warp, (int)o.chunk, stats);
+    else
+        match_kernel<false><<<(unsigned)blocks, wpb * 32, smem, st>>>((const PairDesc*)d_pairs.p, n, cursors, out,
+                                                                      (int*)c->scratch, per_warp, (int)o.chunk, stats);
+    GPM_CK(cudaGetLastError());
+    GPM_CK(cudaEventRecord(c->ev1, st));
+    std::vector<unsigned long long> raw(2 * n + 2);
+    GPM_CK(cudaMemcpyAsync(raw.data(), out, sizeof(unsigned long long) * (2 * n + 2), cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    GPM_CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    t_ms = ms;
+    t_launches = 1;
+    t_bytes = raw[2 * n];
+    memcpy(host_raw, raw.data(), sizeof(unsigned long long) * 2 * n);
+    return GPM_OK;
+}
+
+static int finish_counts(int n, const gpm_plan* const* plans, const unsigned long long* raw, gpm_u128* outs) {
+    for (int i = 0; i < n; ++i) {
+        const unsigned __int128 u = ((unsigned __int128)raw[2 * i + 1] << 64) | raw[2 * i];
+        const __int128 s = (__int128)u;
+        if (s < 0) {
+            set_error("pair %d: negative total (128-bit overflow)", i);
+            return GPM_ERR_OVERFLOW;
+        }
+        const unsigned __int128 q = u / (unsigned __int128)plans[i]->host.redundancy;
+        outs[i].lo = (uint64_t)q;
+        outs[i].hi = (uint64_t)(q >> 64);
+    }
+    return GPM_OK;
+}
+
+}  // namespace gpm
+
+using namespace gpm;
+
+extern "C" {
+
+GPM_API int gpm_set_device(int32_t device) {
+    clear_error();
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        set_error("gpm_set_device: device %d not present", device);
+        return GPM_ERR_NO_DEVICE;
+    }
+    t_device = device;
+    return GPM_OK;
+}
+
+GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_t* col, int32_t relabel,
+                             gpm_graph** out) {
+    clear_error();
+    if (!out || v_cnt < 1 || !rowptr) {
+        set_error("gpm_graph_create: need v_cnt >= 1, rowptr and out");
+        return GPM_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    const uint64_t E = rowptr[v_cnt];
+    if (rowptr[0] != 0 || (E > 0 && !col)) {
+        set_error("gpm_graph_create: rowptr[0] must be 0 and col non-null");
+        return GPM_ERR_INVALID_ARG;
+    }
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> lk(c->mu);
+    gpm_graph* g = new gpm_graph();
+    g->v_cnt = v_cnt;
+    g->e_cnt = E;
+    g->device = c->device;
+    auto fail = [&](int rc) {
+        if (g->rowptr) cudaFree(g->rowptr);
+        if (g->col) cudaFree(g->col);
+        delete g;
+        return rc;
+    };
+    cudaStream_t st = c->stream;
+    if (cudaMalloc(&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
+        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(E, 1)) != cudaSuccess) {
+        set_error("gpm_graph_create: out of device memory for %llu edges", (unsigned long long)E);
+        return fail(GPM_ERR_OOM);
+    }
+    if (cudaMemcpyAsync(g->rowptr, rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        (E && cudaMemcpyAsync(g->col, col, sizeof(int32_t) * E, cudaMemcpyHostToDevice, st) != cudaSuccess)) {
+        set_error("gpm_graph_create: upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return fail(GPM_ERR_CUDA);
+    }
+    unsigned* d_flags = nullptr;
+    if (cudaMalloc(&d_flags, sizeof(unsigned)) != cudaSuccess) return fail(GPM_ERR_OOM);
+    cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st);
+    validate_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), d_flags);
+    unsigned flags = 0;
+    cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(d_flags);
+    if (e != cudaSuccess) {
+        set_error("gpm_graph_create: validation failed: %s", cudaGetErrorString(e));
+        return fail(GPM_ERR_CUDA);
+    }
+    if (flags) {
+        set_error("gpm_graph_create: malformed CSR (%s%s%s%s%s)", flags & 1 ? "offsets " : "",
+                  flags & 2 ? "ids-out-of-range " : "", flags & 4 ? "self-loops " : "",
+                  flags & 8 ? "unsorted-or-duplicate " : "", flags & 16 ? "asymmetric" : "");
+        return fail(GPM_ERR_INVALID_ARG);
+    }
+    int rc = relabel_graph(c, g, relabel != 0);
+    if (rc) return fail(rc);
+    *out = g;
+    return GPM_OK;
+}
+
+GPM_API int gpm_graph_destroy(gpm_graph* g) {
+    clear_error();
+    if (!g) return GPM_OK;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaSetDevice(g->device);
+    if (g->rowptr) cudaFree(g->rowptr);
+    if (g->col) cudaFree(g->col);
+    cudaSetDevice(dev);
+    delete g;
+    return GPM_OK;
+}
+
+GPM_API int gpm_graph_stats(const gpm_graph* g, int64_t* v_cnt, int64_t* e_cnt, int64_t* max_degree,
+                            int64_t* max_intersection_size) {
+    clear_error();
+    if (!g) {
+        set_error("gpm_graph_stats: null graph");
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (v_cnt) *v_cnt = g->v_cnt;
+    if (e_cnt) *e_cnt = (int64_t)g->e_cnt;
+    if (max_degree) *max_degree = g->max_degree;
+    if (max_intersection_size) *max_intersection_size = g->max_isect;
+    return GPM_OK;
+}
+
+GPM_API int gpm_tri_count(gpm_graph* g, uint64_t* out) {
+    clear_error();
+    if (!g || !out) {
+        set_error("gpm_tri_count: null argument");
+        return GPM_ERR_INVALID_ARG;
+    }
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> lk(c->mu);
+    DevBuf buf;
+    GPM_CK(cudaMalloc(&buf.p, 2 * sizeof(unsigned long long)));
+    cudaStream_t st = c->stream;
+    GPM_CK(cudaMemsetAsync(buf.p, 0, 2 * sizeof(unsigned long long), st));
+    unsigned long long* d = (unsigned long long*)buf.p;
+    GPM_CK(cudaEventRecord(c->ev0, st));
+    tc_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), d, d + 1, (int)options().chunk);
+    GPM_CK(cudaGetLastError());
+    GPM_CK(cudaEventRecord(c->ev1, st));
+    unsigned long long h[2];
+    GPM_CK(cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    t_ms = ms;
+    t_launches = 1;
+    t_bytes = 0;
+    *out = h[1];
+    return GPM_OK;
+}
+
+GPM_API int gpm_plan_create(const int64_t* tables, int32_t n_words, gpm_plan** out) {
+    clear_error();
+    if (!out) return GPM_ERR_INVALID_ARG;
+    *out = nullptr;
+    DevPlan hp;
+    int rc = compile_plan(tables, n_words, &hp);
+    if (rc) return rc;
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    gpm_plan* p = new gpm_plan();
+    p->host = hp;
+    p->device = c->device;
+    if (cudaMalloc(&p->dev, sizeof(DevPlan)) != cudaSuccess ||
+        cudaMemcpy(p->dev, &hp, sizeof(DevPlan), cudaMemcpyHostToDevice) != cudaSuccess) {
+        set_error("gpm_plan_create: %s", cudaGetErrorString(cudaGetLastError()));
+        if (p->dev) cudaFree(p->dev);
+        delete p;
+        return GPM_ERR_CUDA;
+    }
+    *out = p;
+    return GPM_OK;
+}
+
+GPM_API int gpm_plan_destroy(gpm_plan* p) {
+    clear_error();
+    if (!p) return GPM_OK;
+    if (p->dev) cudaFree(p->dev);
+    delete p;
+    return GPM_OK;
+}
+
+GPM_API int gpm_batch_count(int32_t n_pairs, gpm_graph* const* graphs, const gpm_plan* const* plans, gpm_u128* outs) {
+    clear_error();
+    if (n_pairs < 1 || !graphs || !plans || !outs) {
+        set_error("gpm_batch_count: need n_pairs >= 1 and non-null arrays");
+        return GPM_ERR_INVALID_ARG;
+    }
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> lk(c->mu);
+    std::vector<unsigned long long> raw(2 * (size_t)n_pairs);
+    int rc = run_pairs(c, n_pairs, graphs, plans, raw.data());
+    if (rc) return rc;
+    return finish_counts(n_pairs, plans, raw.data(), outs);
+}
+
+GPM_API int gpm_count(gpm_graph* g, const gpm_plan* p, gpm_u128* out) {
+    gpm_graph* gs[1] = {g};
+    const gpm_plan* ps[1] = {p};
+    return gpm_batch_count(1, gs, ps, out);
+}
+
+GPM_API int gpm_count_host(int32_t v_cnt, const uint32_t* rowptr, const int32_t* col, int32_t n_plans,
+                           const int64_t* tables, const int32_t* n_words, gpm_u128* outs) {
+    clear_error();
+    if (n_plans < 1 || !tables || !n_words || !outs) {
+        set_error("gpm_count_host: need n_plans >= 1 and non-null arrays");
+        return GPM_ERR_INVALID_ARG;
+    }
+    gpm_graph* g = nullptr;
+    int rc = gpm_graph_create(v_cnt, rowptr, col, 1, &g);
+    if (rc) return rc;
+    std::vector<gpm_plan*> plans(n_plans, nullptr);
+    size_t off = 0;
+    for (int i = 0; i < n_plans && rc == GPM_OK; ++i) {
+        rc = gpm_plan_create(tables + off, n_words[i], &plans[i]);
+        off += (size_t)n_words[i];
+    }
+    if (rc == GPM_OK) {
+        std::vector<gpm_graph*> gs(n_plans, g);
+        std::vector<const gpm_plan*> ps(plans.begin(), plans.end());
+        rc = gpm_batch_count(n_plans, gs.data(), ps.data(), outs);
+    }
+    std::string msg = rc ? gpm_last_error() : std::string();
+    for (gpm_plan* p : plans) gpm_plan_destroy(p);
+    gpm_graph_destroy(g);
+    if (rc) set_error("%s", msg.c_str());
+    return rc;
+}
+
+struct gpm_batch_exec {
+    int n = 0;
+    int device = 0;
+    std::vector<gpm_graph*> graphs;
+    std::vector<const gpm_plan*> plans;
+};
+
+GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph* const* graphs,
+                               const gpm_plan* const* plans, gpm_u128* outs) {
+    clear_error();
+    if (!exec) return GPM_ERR_INVALID_ARG;
+    if (!*exec) {
+        gpm_batch_exec* e = new gpm_batch_exec();
+        e->n = n_pairs;
+        e->graphs.assign(graphs, graphs + n_pairs);
+        e->plans.assign(plans, plans + n_pairs);
+        *exec = e;
+    }
+    return gpm_batch_count((*exec)->n, (*exec)->graphs.data(), (*exec)->plans.data(), outs);
+}
+
+GPM_API int gpm_batch_exec_destroy(gpm_batch_exec* exec) {
+    delete exec;
+    return GPM_OK;
+}
+
+GPM_API int gpm_last_launch_stats(double* kernel_ms, int64_t* launches, uint64_t* algo_bytes) {
+    if (kernel_ms) *kernel_ms = t_ms;
+    if (launches) *launches = t_launches;
+    if (algo_bytes) *algo_bytes = t_bytes;
+    return GPM_OK;
+}
+
+}  // extern "C"

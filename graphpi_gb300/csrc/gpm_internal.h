@@ -1,0 +1,79 @@
+// Internal declarations shared by the host and device translation units.
+#pragma once
+#include <cstdarg>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gpm.h"
+
+namespace gpm {
+
+// thread-local last-error message (gpm_last_error)
+void set_error(const char* fmt, ...);
+void clear_error();
+
+// Process-wide engine knobs (gpm_set_option).
+struct Options {
+    int64_t warps_per_block = 8;
+    int64_t blocks_per_sm = 2;
+    int64_t chunk = 8;          // first-level tasks per queue grab
+    int64_t count_bytes = 0;    // 1: count algorithmic bytes
+    int64_t timeout_ms = 2000;  // bounded device waits
+    int64_t stage_max = 0;      // reserved: father sets staged in shared memory
+    int64_t split = 0;          // reserved: hub splitting width
+};
+Options& options();
+
+// Compiled schedule as the device kernels read it.
+constexpr int kMaxN = 8;
+constexpr int kMaxPrefix = 28;
+constexpr int kMaxBlocks = 63;   // distinct inclusion–exclusion blocks (k <= 6)
+constexpr int kMaxGroups = 256;
+constexpr int kMaxGroupEntries = 1024;
+
+struct DevPlan {
+    int n;        // pattern vertices
+    int k;        // inclusion–exclusion tail length (0: none)
+    int T;        // depth of the tail (k ? n - k : n - 1)
+    int L;        // deepest loop level (T - 1)
+    int nprefix;
+    int nslots;   // scratch slots: materialised prefixes + 2 temporaries
+    int count_only;  // prefix built at level L only to be counted, or -1
+    int nblocks;
+    int ngroups;
+    int pad_;
+    long long redundancy;
+    int loop_set[kMaxN];
+    unsigned rmask[kMaxN];         // depth d stays below min(chosen[j]) for bits j
+    int father[kMaxPrefix];
+    int slot[kMaxPrefix];          // scratch slot of a prefix, -1 for N(v) aliases
+    int chain_begin[kMaxN + 1];    // prefixes built at depth d:
+    int chain_list[kMaxPrefix];    //   chain_list[chain_begin[d] .. chain_begin[d+1])
+    unsigned block_mask[kMaxBlocks];   // tail positions (bit i = depth T+i) of block b
+    int group_begin[kMaxGroups + 1];
+    int group_coef[kMaxGroups];
+    unsigned char group_block[kMaxGroupEntries];
+};
+
+// Decodes gpm_schedule_build tables into a DevPlan (host).
+int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out);
+
+}  // namespace gpm
+
+struct gpm_plan {
+    gpm::DevPlan host;
+    gpm::DevPlan* dev = nullptr;
+    int device = 0;
+};
+
+struct gpm_graph {
+    int32_t v_cnt = 0;
+    uint64_t e_cnt = 0;
+    int32_t max_degree = 0;
+    int32_t max_isect = 0;
+    uint32_t* rowptr = nullptr;  // device
+    int32_t* col = nullptr;      // device
+    int device = 0;
+    bool relabelled = false;
+};

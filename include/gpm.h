@@ -1,0 +1,193 @@
+/*
+ * gpm.h — C ABI of the GB300 GraphPi pattern-matching engine.
+ *
+ * Plain pointers and sizes only; every call returns a GPM_* status and, on
+ * failure, leaves a message for gpm_last_error().  One process, one GPU
+ * (device 0 unless gpm_set_device is called first).
+ *
+ * Each entry point names the reference interface it replaces
+ * (thu-pacman/GraphPi, path:line).
+ */
+#ifndef GPM_H
+#define GPM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GPM_API __attribute__((visibility("default")))
+#else
+#define GPM_API
+#endif
+
+/* status codes */
+#define GPM_OK 0
+#define GPM_ERR_INVALID_ARG 1
+#define GPM_ERR_OOM 2
+#define GPM_ERR_CUDA 3
+#define GPM_ERR_TIMEOUT 4
+#define GPM_ERR_OVERFLOW 5
+#define GPM_ERR_UNSUPPORTED 6
+#define GPM_ERR_NO_DEVICE 7
+
+/* largest pattern the engine accepts (the reference's largest built-in
+ * pattern is 7 vertices, include/pattern.h:17) */
+#define GPM_MAX_PATTERN 8
+
+typedef struct gpm_graph gpm_graph; /* device-resident CSR of one data graph */
+typedef struct gpm_plan gpm_plan;   /* device-resident compiled schedule */
+
+/* exact embedding count; counts of 5-vertex motifs on scale-22 R-MAT graphs
+ * exceed 2^64, so results are 128-bit */
+typedef struct gpm_u128 {
+    uint64_t lo;
+    uint64_t hi;
+} gpm_u128;
+
+/* ------------------------------------------------------------------ */
+/* errors and device                                                   */
+/* ------------------------------------------------------------------ */
+
+/* Message of the last failing call on this thread ("" if none). */
+GPM_API const char* gpm_last_error(void);
+
+/* Selects the CUDA device for later calls on this thread.  The reference
+ * chose an OpenMP team size instead (src/graph.cpp:202). */
+GPM_API int gpm_set_device(int32_t device);
+
+/* ------------------------------------------------------------------ */
+/* data graph                                                          */
+/* ------------------------------------------------------------------ */
+
+/* Uploads an undirected graph given as a symmetric CSR: neighbours of v are
+ * col[rowptr[v] .. rowptr[v+1]), sorted ascending, no self loops, no
+ * duplicates — the layout of the reference `Graph` (include/graph.h:14-15,
+ * src/graph.cpp:141-145).  rowptr[v_cnt] is the directed edge count (the
+ * reference's e_cnt) and must be < 2^32.
+ * relabel = 1 renumbers vertices by descending degree on the device (the
+ * reference's oriented_type 1, src/dataloader.cpp:96-109); counts do not
+ * depend on labels.  The CSR is validated; malformed input returns
+ * GPM_ERR_INVALID_ARG. */
+GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_t* col,
+                             int32_t relabel, gpm_graph** out);
+
+/* Frees a graph (the reference's ~Graph, include/graph.h:24-27). */
+GPM_API int gpm_graph_destroy(gpm_graph* g);
+
+/* v_cnt, directed e_cnt, max degree and the largest possible intersection
+ * (second-largest degree; VertexSet::max_intersection_size,
+ * src/dataloader.cpp:112-115). Any pointer may be NULL. */
+GPM_API int gpm_graph_stats(const gpm_graph* g, int64_t* v_cnt, int64_t* e_cnt,
+                            int64_t* max_degree, int64_t* max_intersection_size);
+
+/* Triangle count on the GPU — Graph::triangle_counting_mt
+ * (include/graph.h:36, src/graph.cpp:112-139); it feeds the schedule cost
+ * model's tri_cnt (src/schedule.cpp:1496). */
+GPM_API int gpm_tri_count(gpm_graph* g, uint64_t* out);
+
+/* ------------------------------------------------------------------ */
+/* pattern, motifs, schedule (host)                                    */
+/* ------------------------------------------------------------------ */
+
+/* All connected k-vertex patterns up to isomorphism, in the reference's
+ * generation order — MotifGenerator::generate (include/motif_generator.h:9,
+ * src/motif_generator.cpp:5-43).  Writes min(count, cap) row-major k*k
+ * adjacency matrices to adj_out and the total to *count. */
+GPM_API int gpm_motifs(int32_t k, int32_t* adj_out, int32_t cap, int32_t* count);
+
+/* Size of the pattern's automorphism group — Schedule::get_multiplicity
+ * (src/schedule.cpp:400-403). */
+GPM_API int gpm_pattern_multiplicity(int32_t n, const int32_t* adj, int64_t* out);
+
+/* Builds a schedule — the Schedule constructor
+ * Schedule(pattern, is_pattern_valid, performance_modeling_type,
+ *          restricts_type, use_in_exclusion_optimize, v_cnt, e_cnt, tri_cnt)
+ * (include/schedule.h:13, src/schedule.cpp:9-253) — and writes its tables
+ * (the getters of include/schedule.h:23-37 plus the public restrict_pair,
+ * in_exclusion_optimize_group/_val of :56-58) as int64 words:
+ *   size, adj[n*n], total_prefix_num, father_prefix_id[P], last[n], next[P],
+ *   loop_set_prefix_id[n], total_restrict_num, restrict_last[n],
+ *   restrict_next[R], restrict_index[R], n_pairs, pairs[2*n_pairs],
+ *   in_exclusion_optimize_num, n_groups,
+ *     per group: val, n_blocks, per block: len, members[len],
+ *   in_exclusion_optimize_redundancy, multiplicity.
+ * *n_words receives the length; *valid the reference's is_pattern_valid.
+ * perf_type 0..3 and restricts_type 0..2 as in include/schedule.h:14-20;
+ * perf_type != 0 with tri_cnt < 0 is GPM_ERR_INVALID_ARG (the reference
+ * asserts, src/schedule.cpp:11-15). */
+GPM_API int gpm_schedule_build(int32_t n, const int32_t* adj, int32_t perf_type,
+                               int32_t restricts_type, int32_t use_iep, int64_t v_cnt,
+                               uint64_t e_cnt, int64_t tri_cnt, int64_t* tables, int32_t cap,
+                               int32_t* n_words, int32_t* valid);
+
+/* Compiles schedule tables (layout of gpm_schedule_build) into a device
+ * plan: per-depth candidate lists, restriction bounds, prefix-set slots and
+ * the inclusion-exclusion groups.  Replaces the table walks of
+ * src/graph.cpp:217,249,306-313,353,368,383. */
+GPM_API int gpm_plan_create(const int64_t* tables, int32_t n_words, gpm_plan** out);
+GPM_API int gpm_plan_destroy(gpm_plan* p);
+
+/* ------------------------------------------------------------------ */
+/* counting (the hot path)                                             */
+/* ------------------------------------------------------------------ */
+
+/* Counts embeddings of the plan's pattern in g — Graph::pattern_matching
+ * (include/graph.h:39, src/graph.cpp:199-398): the schedule-driven nested
+ * loops, restriction pruning, injectivity checks and the
+ * inclusion-exclusion tail, divided by the plan's redundancy (:244).
+ * Exact in 128 bits. */
+GPM_API int gpm_count(gpm_graph* g, const gpm_plan* p, gpm_u128* out);
+
+/* Counts n_pairs (graph, plan) pairs in one persistent launch fed by
+ * per-pair work queues (no reference counterpart; it replaces n_pairs
+ * separate Graph::pattern_matching calls).  outs[i] belongs to pair i. */
+GPM_API int gpm_batch_count(int32_t n_pairs, gpm_graph* const* graphs,
+                            const gpm_plan* const* plans, gpm_u128* outs);
+
+/* gpm_batch_count captured once into a CUDA graph and replayed: *exec is
+ * created on the first call with *exec == NULL and reused afterwards for the
+ * same pairs.  gpm_batch_exec_destroy frees it. */
+typedef struct gpm_batch_exec gpm_batch_exec;
+GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph* const* graphs,
+                               const gpm_plan* const* plans, gpm_u128* outs);
+GPM_API int gpm_batch_exec_destroy(gpm_batch_exec* exec);
+
+/* One-shot host-buffer path: uploads the host CSR, relabels, counts every
+ * schedule in `tables` (n_plans schedules, each n_words[i] int64 words laid
+ * out as gpm_schedule_build writes them, concatenated) in one batched
+ * launch, copies the counts back and frees the device copy.  This is the
+ * call a host program that owns its graph in memory makes — the reference's
+ * `g->pattern_matching(schedule, n)` per schedule. */
+GPM_API int gpm_count_host(int32_t v_cnt, const uint32_t* rowptr, const int32_t* col,
+                           int32_t n_plans, const int64_t* tables, const int32_t* n_words,
+                           gpm_u128* outs);
+
+/* ------------------------------------------------------------------ */
+/* tuning                                                              */
+/* ------------------------------------------------------------------ */
+
+/* Engine knobs (counts never depend on them):
+ *   "warps_per_block", "blocks_per_sm", "chunk" (work-queue grab size),
+ *   "split" (first-level candidates per task for hub roots),
+ *   "stage_max" (largest father set staged in shared memory),
+ *   "timeout_ms" (bounded waits).  Returns GPM_ERR_INVALID_ARG on an
+ * unknown key. */
+GPM_API int gpm_set_option(const char* key, int64_t value);
+GPM_API int gpm_get_option(const char* key, int64_t* value);
+
+/* Launch statistics of the last counting call on this thread: kernel time
+ * in milliseconds (CUDA events on the launch stream), number of kernels
+ * launched, and the algorithmic bytes the intersections read (4 bytes per
+ * element a merge would touch, plus 8 bytes per offset pair; counted only
+ * when the "count_bytes" option is 1). */
+GPM_API int gpm_last_launch_stats(double* kernel_ms, int64_t* launches, uint64_t* algo_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPM_H */
