@@ -346,6 +346,9 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "timeout_ms") slot = &o.timeout_ms, lo = 1, hi = 3600 * 1000;
     else if (k == "stage_max") slot = &o.stage_max, lo = 0, hi = 1 << 16;
     else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
+    else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;
+    else if (k == "stripe") slot = &o.stripe, lo = 0, hi = (1 << 30) - 1;
+    else if (k == "raw_sums") slot = &o.raw_sums, lo = 0, hi = 1;
     if (!slot) {
         set_error("gpm_set_option: unknown key '%s'", key);
         return GPM_ERR_INVALID_ARG;
@@ -370,6 +373,9 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "timeout_ms") *value = o.timeout_ms;
     else if (k == "stage_max") *value = o.stage_max;
     else if (k == "split") *value = o.split;
+    else if (k == "stripes") *value = o.stripes;
+    else if (k == "stripe") *value = o.stripe;
+    else if (k == "raw_sums") *value = o.raw_sums;
     else {
         set_error("gpm_get_option: unknown key '%s'", key);
         return GPM_ERR_INVALID_ARG;

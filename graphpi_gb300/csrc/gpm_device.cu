@@ -384,10 +384,11 @@ struct WarpCtx {
 };
 
 template <bool kBytes>
-__global__ void __launch_bounds__(256) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
+__global__ void __launch_bounds__(512) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
                                                     unsigned long long* __restrict__ cursors,
                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
                                                     long long scratch_per_warp, int chunk,
+                                                    unsigned long long stripes, unsigned long long stripe,
                                                     unsigned long long* __restrict__ stats) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -407,9 +408,11 @@ __global__ void __launch_bounds__(256) match_kernel(const PairDesc* __restrict__
         int cur_v0 = -1;
         unsigned cur_lo = 0, cur_hi = 0;
         for (;;) {
-            unsigned long long t0 = 0;
-            if (lane == 0) t0 = atomicAdd(&cursors[p], (unsigned long long)chunk);
-            t0 = __shfl_sync(kFull, t0, 0);
+            // chunk q of this stripe covers tasks [(q*stripes+stripe)*chunk, +chunk)
+            unsigned long long q = 0;
+            if (lane == 0) q = atomicAdd(&cursors[p], 1ull);
+            q = __shfl_sync(kFull, q, 0);
+            const unsigned long long t0 = (q * stripes + stripe) * (unsigned long long)chunk;
             if (t0 >= pd.ntasks) break;
             const unsigned long long t1 = min(t0 + (unsigned long long)chunk, pd.ntasks);
             for (unsigned long long t = t0; t < t1; ++t) {
@@ -706,7 +709,9 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
         descs[i].g = view_of(g);
         descs[i].plan = p->dev;
         descs[i].ntasks = p->host.T == 1 ? (unsigned long long)g->v_cnt : (unsigned long long)g->e_cnt;
-        descs[i].cap = std::max(1, g->max_isect);
+        // every set built is a subset of one neighbour list: the largest degree
+        // bounds it (inclusion-exclusion temporaries can be N(v0) itself)
+        descs[i].cap = std::max(1, g->max_degree);
         descs[i].pad_ = 0;
         cap = std::max(cap, descs[i].cap);
         nslots = std::max(nslots, p->host.nslots);
@@ -734,11 +739,13 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     const size_t smem = sizeof(WarpState) * wpb;
     GPM_CK(cudaEventRecord(c->ev0, st));
     if (o.count_bytes)
-        match_kernel<true><<<(unsigned)blocks, wpb * 32, smem, st>>>((const PairDesc*)d_pairs.p, n, cursors, out,
-                                                                     (int*)c->scratch, per_warp, (int)o.chunk, stats);
+        match_kernel<true><<<(unsigned)blocks, wpb * 32, smem, st>>>(
+            (const PairDesc*)d_pairs.p, n, cursors, out, (int*)c->scratch, per_warp, (int)o.chunk,
+            (unsigned long long)o.stripes, (unsigned long long)o.stripe, stats);
     else
-        match_kernel<false><<<(unsigned)blocks, wpb * 32, smem, st>>>((const PairDesc*)d_pairs.p, n, cursors, out,
-                                                                      (int*)c->scratch, per_warp, (int)o.chunk, stats);
+        match_kernel<false><<<(unsigned)blocks, wpb * 32, smem, st>>>(
+            (const PairDesc*)d_pairs.p, n, cursors, out, (int*)c->scratch, per_warp, (int)o.chunk,
+            (unsigned long long)o.stripes, (unsigned long long)o.stripe, stats);
     GPM_CK(cudaGetLastError());
     GPM_CK(cudaEventRecord(c->ev1, st));
     std::vector<unsigned long long> raw(2 * n + 2);
@@ -754,6 +761,18 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
 }
 
 static int finish_counts(int n, const gpm_plan* const* plans, const unsigned long long* raw, gpm_u128* outs) {
+    if (options().raw_sums) {
+        // undivided two's-complement sums (partial stripes are summed by the caller)
+        for (int i = 0; i < n; ++i) {
+            outs[i].lo = raw[2 * i];
+            outs[i].hi = raw[2 * i + 1];
+        }
+        return GPM_OK;
+    }
+    if (options().stripes != 1) {
+        set_error("a striped launch covers part of the work: set raw_sums=1 and divide the summed stripes");
+        return GPM_ERR_INVALID_ARG;
+    }
     for (int i = 0; i < n; ++i) {
         const unsigned __int128 u = ((unsigned __int128)raw[2 * i + 1] << 64) | raw[2 * i];
         const __int128 s = (__int128)u;

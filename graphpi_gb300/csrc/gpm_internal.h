@@ -22,6 +22,9 @@ struct Options {
     int64_t timeout_ms = 2000;  // bounded device waits
     int64_t stage_max = 0;      // reserved: father sets staged in shared memory
     int64_t split = 0;          // reserved: hub splitting width
+    int64_t stripes = 1;        // a launch covers chunks q*stripes + stripe only
+    int64_t stripe = 0;
+    int64_t raw_sums = 0;       // 1: return undivided 128-bit sums
 };
 Options& options();
 

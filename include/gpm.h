@@ -174,8 +174,14 @@ GPM_API int gpm_count_host(int32_t v_cnt, const uint32_t* rowptr, const int32_t*
  *   "warps_per_block", "blocks_per_sm", "chunk" (work-queue grab size),
  *   "split" (first-level candidates per task for hub roots),
  *   "stage_max" (largest father set staged in shared memory),
- *   "timeout_ms" (bounded waits).  Returns GPM_ERR_INVALID_ARG on an
- * unknown key. */
+ *   "timeout_ms" (bounded waits),
+ *   "stripes"/"stripe" (a launch covers only work chunks q*stripes+stripe:
+ *   the first-level tasks split into `stripes` interleaved parts, e.g. one
+ *   per GPU or per bounded step), "raw_sums" (1: outputs are the undivided
+ *   signed 128-bit sums, to be added over stripes and then divided by the
+ *   schedule's redundancy; required when stripes > 1),
+ *   "count_bytes" (1: count algorithmic bytes).  Returns
+ * GPM_ERR_INVALID_ARG on an unknown key or out-of-range value. */
 GPM_API int gpm_set_option(const char* key, int64_t value);
 GPM_API int gpm_get_option(const char* key, int64_t* value);
 

@@ -1,0 +1,116 @@
+"""Pins the CPU oracle: against the reference's recorded outputs (golden
+fixtures), against the reference library itself where it was built here,
+and against the definition-level brute-force counter."""
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import graphpi_gb300 as gp
+from graphpi_gb300 import workloads
+from tests.oracle_lib import REF_LIB, csr_checksum, golden
+
+COUNTS = golden("counts.json")
+WIKI = Path("/root/reference/dataset/wiki-vote_input")
+
+GEN = {
+    "chung_lu_7k": workloads.chung_lu_7k,
+    "rmat_s10": lambda: gp.rmat(10, 16, 0.57, 0.19, 0.19, 2),
+    "chung_lu_2k": lambda: gp.chung_lu(2000, 12.0, 2.3, 300, 7),
+    "rmat_s12_noiep": lambda: gp.rmat(12, 8, 0.57, 0.19, 0.19, 5),
+}
+
+
+@pytest.mark.parametrize("name", list(GEN))
+def test_generator_reproduces_golden_graph(engine, name):
+    g = GEN[name]()
+    e = COUNTS["graphs"][name]
+    assert (g.v_cnt, g.e_cnt) == (e["v_cnt"], e["e_cnt"])
+    assert csr_checksum(g) == e["checksum"]
+
+
+@pytest.mark.parametrize("name", list(GEN))
+def test_oracle_matches_reference_counts(engine, oracle, name):
+    g = GEN[name]()
+    e = COUNTS["graphs"][name]
+    assert oracle.triangles(g) == e["tri_cnt"]
+    perf, restr, iep = e["flags"]
+    for pname, want in e["counts"].items():
+        n = int(round(len(e["adj"][pname]) ** 0.5))
+        p = gp.Pattern.from_adj(np.array(e["adj"][pname]).reshape(n, n))
+        s = gp.Schedule(p, perf, restr, bool(iep), g.v_cnt, g.e_cnt, e["tri_cnt"])
+        assert oracle.count(g, s) == want, pname
+
+
+def test_oracle_matches_brute_force(engine, oracle):
+    g = gp.chung_lu(250, 10.0, 2.2, 60, 11)
+    tri = oracle.triangles(g)
+    for k in (3, 4, 5):
+        for p in gp.MotifGenerator(k).generate():
+            for flags in [(1, 1, True), (0, 0, False), (1, 1, False)]:
+                s = gp.Schedule(p, flags[0], flags[1], flags[2], g.v_cnt, g.e_cnt, tri)
+                if not s.is_pattern_valid:
+                    continue
+                want = oracle.brute_force(g, p)
+                got = oracle.count(g, s)
+                if flags[1] == 0:  # no restrictions: every automorphic copy counted
+                    got //= p.multiplicity()
+                assert got == want, (p, flags)
+
+
+def test_oracle_triangles_closed_forms(engine, oracle):
+    k = gp.complete_graph(9)
+    assert oracle.triangles(k) == 84
+    assert oracle.count(k, gp.Schedule(gp.Pattern(4, True), 1, 1, True, 9, k.e_cnt, 84)) == 126
+
+
+def test_oracle_root_shards_sum_to_total(engine, oracle):
+    g = gp.chung_lu(600, 9.0, 2.2, 100, 3)
+    tri = oracle.triangles(g)
+    for p in [gp.Pattern(gp.PatternType.House), gp.Pattern(gp.PatternType.Rectangle)]:
+        s = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri)
+        full = oracle.raw_roots(g, s, np.arange(g.v_cnt))
+        shards = sum(oracle.raw_roots(g, s, np.arange(r, g.v_cnt, 3)) for r in range(3))
+        assert full == shards
+        assert full // s.get_in_exclusion_optimize_redundancy() == oracle.count(g, s)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="reference library not built here")
+def test_oracle_matches_live_reference(engine, oracle):
+    R = C.CDLL(str(REF_LIB))
+    R.ref_graph_from_csr.restype = C.c_void_p
+    R.ref_graph_from_csr.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int]
+    R.ref_graph_tri.restype = C.c_longlong
+    R.ref_graph_tri.argtypes = [C.c_void_p]
+    R.ref_graph_free.argtypes = [C.c_void_p]
+    R.ref_schedule_create.restype = C.c_void_p
+    R.ref_schedule_create.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint,
+                                      C.c_longlong, C.POINTER(C.c_int)]
+    R.ref_schedule_free.argtypes = [C.c_void_p]
+    R.ref_pattern_matching.restype = C.c_longlong
+    R.ref_pattern_matching.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    g = gp.rmat(11, 8, 0.57, 0.19, 0.19, 9)
+    rg = R.ref_graph_from_csr(g.v_cnt, g.vertex.ctypes.data, g.edge.ctypes.data, -1, 4)
+    tri = R.ref_graph_tri(rg)
+    assert tri == oracle.triangles(g)
+    for p in gp.motifs_3_to_5()[:12]:
+        a = np.ascontiguousarray(p.adj, dtype=np.int32)
+        ok = C.c_int()
+        rs = R.ref_schedule_create(a.shape[0], a.ctypes.data, 1, 1, 1, g.v_cnt, g.e_cnt, tri, C.byref(ok))
+        want = R.ref_pattern_matching(rg, rs, 4)
+        R.ref_schedule_free(rs)
+        s = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri)
+        assert oracle.count(g, s) == want
+    R.ref_graph_free(rg)
+
+
+@pytest.mark.skipif(not WIKI.exists(), reason="Wiki-Vote dataset only in the reference checkout")
+def test_oracle_wiki_vote(engine, oracle):
+    g = gp.DataLoader().load_data(gp.DataType.Wiki_Vote, str(WIKI))
+    w = COUNTS["wiki_vote"]
+    assert (g.v_cnt, g.e_cnt) == (7115, 201524)
+    assert oracle.triangles(g) == w["tri_cnt"]
+    for name, p in [("rectangle", gp.Pattern(gp.PatternType.Rectangle)), ("clique4", gp.Pattern(4, True))]:
+        s = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, g.tri_cnt)
+        assert oracle.count(g, s) == w[name]
