@@ -208,6 +208,13 @@ class Schedule:
         if pos != len(t):
             raise ValueError("schedule tables have trailing words")
 
+    def label_sensitive(self) -> bool:
+        """True when the count depends on vertex labels (gpm_schedule_analyze)."""
+        t = np.ascontiguousarray(self.tables, dtype=np.int64)
+        out = C.c_int32()
+        check(lib().gpm_schedule_analyze(t.ctypes.data, len(t), C.byref(out)), "gpm_schedule_analyze")
+        return bool(out.value)
+
     # reference getters (include/schedule.h:23-37)
     def get_size(self): return self.size
     def get_total_prefix_num(self): return self.total_prefix_num

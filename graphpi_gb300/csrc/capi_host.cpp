@@ -226,8 +226,187 @@ int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out) {
         set_error("gpm_plan_create: inclusion-exclusion length %d without groups", k);
         return GPM_ERR_INVALID_ARG;
     }
+    p.label_sensitive = plan_label_sensitive(p);
     *out = p;
     return GPM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host model of the enumeration.  The reference's inclusion–exclusion tail
+// skips the restrictions of its own loops and divides by a redundancy
+// measured on K_n (src/graph.cpp:306-344, src/schedule.cpp:1746-1764).
+// When a skipped restriction ties a tail loop to an earlier loop, the
+// overcount differs from prefix to prefix and the reference's result depends
+// on the vertex labels (some 6-vertex patterns, e.g. K3,3 and the hourglass,
+// are off from the true count).  Such plans must see the caller's labels to
+// reproduce the reference's output; the check below counts each plan on
+// small random graphs under several labellings.
+
+namespace {
+
+struct ProbeDfs {
+    const DevPlan& p;
+    int V;
+    const std::vector<uint32_t>& rp;
+    const std::vector<int32_t>& col;
+    std::vector<std::vector<int> > sets;
+    int chosen[kMaxN];
+    __int128 acc = 0;
+
+    ProbeDfs(const DevPlan& plan, int v, const std::vector<uint32_t>& r, const std::vector<int32_t>& c)
+        : p(plan), V(v), rp(r), col(c), sets(kMaxPrefix) {}
+
+    std::vector<int> nbr(int v) const { return std::vector<int>(col.begin() + rp[v], col.begin() + rp[v + 1]); }
+
+    int bound(int d) const {
+        int b = V;
+        for (int j = 0; j < d; ++j)
+            if (p.rmask[d] >> j & 1) b = std::min(b, chosen[j]);
+        return b;
+    }
+
+    long long outside(const std::vector<int>& S, size_t len, int nch) const {
+        long long r = (long long)len;
+        for (int j = 0; j < nch; ++j)
+            if (std::binary_search(S.begin(), S.begin() + len, chosen[j])) --r;
+        return r;
+    }
+
+    bool build(int d, int v) {
+        std::vector<int> nv = nbr(v);
+        for (int c = p.chain_begin[d]; c < p.chain_begin[d + 1]; ++c) {
+            const int pid = p.chain_list[c], f = p.father[pid];
+            if (f < 0) {
+                sets[pid] = nv;
+            } else {
+                std::vector<int> o;
+                std::set_intersection(sets[f].begin(), sets[f].end(), nv.begin(), nv.end(), std::back_inserter(o));
+                sets[pid].swap(o);
+            }
+            if (sets[pid].empty()) return false;
+        }
+        return true;
+    }
+
+    __int128 tail() {
+        const int T = p.T;
+        const std::vector<int>& S = sets[p.loop_set[T]];
+        if (S.empty()) return 0;
+        if (!p.k) {
+            size_t lb = std::lower_bound(S.begin(), S.end(), bound(T)) - S.begin();
+            return outside(S, lb, T);
+        }
+        long long bv[kMaxBlocks];
+        for (int b = 0; b < p.nblocks; ++b) {
+            std::vector<int> a;
+            bool first = true;
+            for (int i = 0; i < p.k; ++i) {
+                if (!(p.block_mask[b] >> i & 1)) continue;
+                const std::vector<int>& Si = sets[p.loop_set[T + i]];
+                if (first) {
+                    a = Si;
+                    first = false;
+                } else {
+                    std::vector<int> o;
+                    std::set_intersection(a.begin(), a.end(), Si.begin(), Si.end(), std::back_inserter(o));
+                    a.swap(o);
+                }
+            }
+            bv[b] = outside(a, a.size(), T);
+        }
+        __int128 total = 0;
+        for (int g = 0; g < p.ngroups; ++g) {
+            __int128 v = p.group_coef[g];
+            for (int q = p.group_begin[g]; q < p.group_begin[g + 1]; ++q) v *= bv[p.group_block[q]];
+            total += v;
+        }
+        return total;
+    }
+
+    void level(int d) {
+        if (d == p.T) {
+            acc += tail();
+            return;
+        }
+        const std::vector<int> S = sets[p.loop_set[d]];
+        const int b = bound(d);
+        for (int v : S) {
+            if (v >= b) break;
+            bool dup = false;
+            for (int j = 0; j < d; ++j) dup |= chosen[j] == v;
+            if (dup || !build(d, v)) continue;
+            chosen[d] = v;
+            level(d + 1);
+        }
+    }
+};
+
+// Erdős–Rényi graph from a fixed seed, relabelled by perm.
+void probe_graph(int n, double prob, uint64_t seed, const std::vector<int>& perm, std::vector<uint32_t>& rp,
+                 std::vector<int32_t>& col) {
+    std::vector<std::vector<int> > adj(n);
+    uint64_t x = seed;
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            x = x * 6364136223846793005ull + 1442695040888963407ull;
+            if ((double)(x >> 11) / 9007199254740992.0 < prob) {
+                adj[perm[i]].push_back(perm[j]);
+                adj[perm[j]].push_back(perm[i]);
+            }
+        }
+    rp.assign(n + 1, 0);
+    col.clear();
+    for (int i = 0; i < n; ++i) {
+        std::sort(adj[i].begin(), adj[i].end());
+        col.insert(col.end(), adj[i].begin(), adj[i].end());
+        rp[i + 1] = (uint32_t)col.size();
+    }
+}
+
+}  // namespace
+
+__int128 plan_probe_count(const DevPlan& p, int v_cnt, const std::vector<uint32_t>& rowptr,
+                          const std::vector<int32_t>& col) {
+    ProbeDfs dfs(p, v_cnt, rowptr, col);
+    for (int v = 0; v < v_cnt; ++v) {
+        dfs.chosen[0] = v;
+        if (!dfs.build(0, v)) continue;
+        dfs.level(1);
+    }
+    return dfs.acc;
+}
+
+int plan_label_sensitive(const DevPlan& p) {
+    // without skipped restrictions every valid schedule counts exactly
+    bool skipped = false;
+    for (int d = p.T; d < p.n && p.k; ++d) skipped |= p.rmask[d] != 0;
+    if (!skipped) return 0;
+    static std::mutex mu;
+    static std::map<std::string, int> memo;
+    std::string key((const char*)&p, sizeof(DevPlan));
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = memo.find(key);
+        if (it != memo.end()) return it->second;
+    }
+    int sensitive = 0;
+    const int sizes[3] = {10, 12, 13};
+    for (int gi = 0; gi < 3 && !sensitive; ++gi) {
+        const int n = sizes[gi];
+        std::vector<int> ident(n), rev(n), mix(n);
+        for (int i = 0; i < n; ++i) ident[i] = i, rev[i] = n - 1 - i, mix[i] = (i * 7 + 3) % n;
+        std::vector<uint32_t> rp;
+        std::vector<int32_t> col;
+        probe_graph(n, 0.55, 0x5eed0000ull + gi, ident, rp, col);
+        const __int128 base = plan_probe_count(p, n, rp, col);
+        for (const auto* perm : {&rev, &mix}) {
+            probe_graph(n, 0.55, 0x5eed0000ull + gi, *perm, rp, col);
+            if (plan_probe_count(p, n, rp, col) != base) sensitive = 1;
+        }
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    memo[key] = sensitive;
+    return sensitive;
 }
 
 }  // namespace gpm
@@ -330,6 +509,16 @@ GPM_API int gpm_schedule_build(int32_t n, const int32_t* adj, int32_t perf_type,
         set_error("gpm_schedule_build: %s", e.what());
         return GPM_ERR_INVALID_ARG;
     }
+}
+
+GPM_API int gpm_schedule_analyze(const int64_t* tables, int32_t n_words, int32_t* label_sensitive) {
+    gpm::clear_error();
+    if (!label_sensitive) return GPM_ERR_INVALID_ARG;
+    gpm::DevPlan p;
+    int rc = gpm::compile_plan(tables, n_words, &p);
+    if (rc) return rc;
+    *label_sensitive = p.label_sensitive;
+    return GPM_OK;
 }
 
 GPM_API int gpm_set_option(const char* key, int64_t value) {

@@ -89,6 +89,48 @@ __device__ __forceinline__ int lower_bound_u(const int* __restrict__ a, int n, i
     return lo;
 }
 
+// Merge variant: both lists advance through 32-wide coalesced windows; each
+// lane locates its A element in the B window with a 5-step shuffle search.
+// Elements of A no larger than the last B of the window are resolved and
+// consumed, likewise for B, so each step consumes a full window of at least
+// one list.  Found elements are compacted in order (kStore) or counted minus
+// the chosen vertices.
+template <bool kStore>
+__device__ int warp_merge(const int* __restrict__ A, int na, const int* __restrict__ B, int nb,
+                          int* __restrict__ out, const int* chosen, int nch, int lane) {
+    int i = 0, j = 0, acc = 0;
+    while (i < na && j < nb) {
+        const int a = (i + lane < na) ? A[i + lane] : INT_MAX;
+        const int b = (j + lane < nb) ? B[j + lane] : INT_MAX;
+        int pos = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int bv = __shfl_sync(kFull, b, pos + step - 1);
+            if (bv < a) pos += step;
+        }
+        bool found = (a != INT_MAX) && (__shfl_sync(kFull, b, pos) == a);
+        if (!kStore && found)
+            for (int q = 0; q < nch; ++q)
+                if (chosen[q] == a) found = false;
+        const unsigned fm = __ballot_sync(kFull, found);
+        if (kStore && found) out[acc + __popc(fm & lanemask_lt())] = a;
+        acc += __popc(fm);
+        const int amax = __shfl_sync(kFull, a, 31), bmax = __shfl_sync(kFull, b, 31);
+        i += __popc(__ballot_sync(kFull, a <= bmax));
+        j += __popc(__ballot_sync(kFull, b <= amax));
+    }
+    if (kStore) __syncwarp();
+    return acc;
+}
+
+// Merge when both lists are of similar length: a binary-search round costs
+// about log2(nb) dependent loads for 32 elements of the short list, a merge
+// step one coalesced load per list for at least 32 elements.
+__device__ __forceinline__ bool prefer_merge(int na, int nb) {
+    const int lg = 32 - __clz(nb | 1);
+    return (long long)na * lg >= (long long)(na + nb);
+}
+
 // A ∩ B written sorted to out; returns its size.
 __device__ int isect_store(const int* __restrict__ A, int na, const int* __restrict__ B, int nb,
                            int* __restrict__ out, int lane) {
@@ -96,6 +138,7 @@ __device__ int isect_store(const int* __restrict__ A, int na, const int* __restr
         const int* t = A; A = B; B = t;
         int u = na; na = nb; nb = u;
     }
+    if (prefer_merge(na, nb)) return warp_merge<true>(A, na, B, nb, out, nullptr, 0, lane);
     int written = 0, lo = 0;
     for (int base = 0; base < na; base += 32) {
         const int i = base + lane;
@@ -126,6 +169,7 @@ __device__ int isect_count(const int* __restrict__ A, int na, const int* __restr
         const int* t = A; A = B; B = t;
         int u = na; na = nb; nb = u;
     }
+    if (prefer_merge(na, nb)) return warp_merge<false>(A, na, B, nb, nullptr, chosen, nch, lane);
     int cnt = 0, lo = 0;
     for (int base = 0; base < na; base += 32) {
         const int i = base + lane;
@@ -668,8 +712,9 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     GPM_CK(cub::DeviceSegmentedSort::SortKeys(tmp3.p, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
                                               (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
     GPM_CK(cudaStreamSynchronize(st));
-    cudaFree(g->rowptr);
-    cudaFree(g->col);
+    // the caller's ids stay resident for label-sensitive plans
+    g->orig_rowptr = g->rowptr;
+    g->orig_col = g->col;
     g->rowptr = (uint32_t*)new_rowptr.p;
     new_rowptr.p = nullptr;
     g->col = (int32_t*)new_col.p;
@@ -678,10 +723,10 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     return GPM_OK;
 }
 
-static GraphView view_of(const gpm_graph* g) {
+static GraphView view_of(const gpm_graph* g, bool caller_ids = false) {
     GraphView v;
-    v.rowptr = g->rowptr;
-    v.col = g->col;
+    v.rowptr = caller_ids && g->orig_rowptr ? g->orig_rowptr : g->rowptr;
+    v.col = caller_ids && g->orig_col ? g->orig_col : g->col;
     v.v_cnt = g->v_cnt;
     v.pad_ = 0;
     v.e_cnt = g->e_cnt;
@@ -706,7 +751,7 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
             set_error("pair %d: graph/plan live on another device", i);
             return GPM_ERR_INVALID_ARG;
         }
-        descs[i].g = view_of(g);
+        descs[i].g = view_of(g, p->host.label_sensitive != 0);
         descs[i].plan = p->dev;
         descs[i].ntasks = p->host.T == 1 ? (unsigned long long)g->v_cnt : (unsigned long long)g->e_cnt;
         // every set built is a subset of one neighbour list: the largest degree
@@ -826,6 +871,8 @@ GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_
     g->e_cnt = E;
     g->device = c->device;
     auto fail = [&](int rc) {
+        if (g->orig_rowptr && g->orig_rowptr != g->rowptr) cudaFree(g->orig_rowptr);
+        if (g->orig_col && g->orig_col != g->col) cudaFree(g->orig_col);
         if (g->rowptr) cudaFree(g->rowptr);
         if (g->col) cudaFree(g->col);
         delete g;
@@ -873,6 +920,8 @@ GPM_API int gpm_graph_destroy(gpm_graph* g) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaSetDevice(g->device);
+    if (g->orig_rowptr && g->orig_rowptr != g->rowptr) cudaFree(g->orig_rowptr);
+    if (g->orig_col && g->orig_col != g->col) cudaFree(g->orig_col);
     if (g->rowptr) cudaFree(g->rowptr);
     if (g->col) cudaFree(g->col);
     cudaSetDevice(dev);

@@ -45,7 +45,7 @@ struct DevPlan {
     int count_only;  // prefix built at level L only to be counted, or -1
     int nblocks;
     int ngroups;
-    int pad_;
+    int label_sensitive;  // 1: the count depends on vertex labels; run on the caller's ids
     long long redundancy;
     int loop_set[kMaxN];
     unsigned rmask[kMaxN];         // depth d stays below min(chosen[j]) for bits j
@@ -62,6 +62,15 @@ struct DevPlan {
 // Decodes gpm_schedule_build tables into a DevPlan (host).
 int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out);
 
+// Host model of the device enumeration for a plan on a small CSR: the raw
+// signed sum before the division by the redundancy.
+__int128 plan_probe_count(const DevPlan& p, int v_cnt, const std::vector<uint32_t>& rowptr,
+                          const std::vector<int32_t>& col);
+
+// 1 when the plan's count changes with the vertex labelling (see
+// compile_plan), 0 otherwise.
+int plan_label_sensitive(const DevPlan& p);
+
 }  // namespace gpm
 
 struct gpm_plan {
@@ -75,8 +84,10 @@ struct gpm_graph {
     uint64_t e_cnt = 0;
     int32_t max_degree = 0;
     int32_t max_isect = 0;
-    uint32_t* rowptr = nullptr;  // device
+    uint32_t* rowptr = nullptr;  // device, relabelled by degree when relabelled
     int32_t* col = nullptr;      // device
+    uint32_t* orig_rowptr = nullptr;  // device, the caller's ids (== rowptr when not relabelled)
+    int32_t* orig_col = nullptr;
     int device = 0;
     bool relabelled = false;
 };

@@ -50,6 +50,7 @@ SIGNATURES = {
     "gpm_motifs": (I32, [I32, P, I32, PI32]),
     "gpm_pattern_multiplicity": (I32, [I32, P, PI64]),
     "gpm_schedule_build": (I32, [I32, P, I32, I32, I32, I64, U64, I64, P, I32, PI32, PI32]),
+    "gpm_schedule_analyze": (I32, [P, I32, PI32]),
     "gpm_plan_create": (I32, [P, I32, C.POINTER(P)]),
     "gpm_plan_destroy": (I32, [P]),
     "gpm_count": (I32, [P, P, C.POINTER(U128)]),

@@ -124,6 +124,16 @@ GPM_API int gpm_schedule_build(int32_t n, const int32_t* adj, int32_t perf_type,
                                uint64_t e_cnt, int64_t tri_cnt, int64_t* tables, int32_t cap,
                                int32_t* n_words, int32_t* valid);
 
+/* Host-side analysis of schedule tables: *label_sensitive = 1 when the
+ * schedule's count depends on the vertex labelling.  The reference's
+ * inclusion–exclusion tail skips the restrictions of its own loops and
+ * divides by a redundancy measured on K_n (src/graph.cpp:306-344,
+ * src/schedule.cpp:1746-1764); when a skipped restriction ties a tail loop
+ * to an earlier loop the result varies with the labels (and differs from
+ * the true count).  Counting runs such schedules on the caller's vertex ids,
+ * never on the degree-relabelled copy, so results equal the reference's. */
+GPM_API int gpm_schedule_analyze(const int64_t* tables, int32_t n_words, int32_t* label_sensitive);
+
 /* Compiles schedule tables (layout of gpm_schedule_build) into a device
  * plan: per-depth candidate lists, restriction bounds, prefix-set slots and
  * the inclusion-exclusion groups.  Replaces the table walks of

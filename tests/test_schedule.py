@@ -88,3 +88,16 @@ def test_builtin_patterns(engine):
         assert p.check_connected()
         s = gp.Schedule(p, 0, 1, True, 1000, 10000, 0)
         assert s.is_pattern_valid
+
+
+def test_label_sensitive_schedules_flagged(engine):
+    # schedules whose reference count depends on labels (checked against the
+    # brute-force count: these differ from it) must be flagged
+    wrong = ["011100100011100011100011011100011100", "011100101010110001100011010101001110",
+             "011110101110110101111001110001001110", "011111101100110010110001101001100110"]
+    for adj in wrong:
+        s = gp.Schedule(gp.Pattern(6, adj), 1, 1, True, 400, 3000, 2000)
+        assert s.label_sensitive(), adj
+    # without inclusion-exclusion nothing is skipped
+    for p in gp.motifs_3_to_5():
+        assert not gp.Schedule(p, 1, 1, False, 400, 3000, 2000).label_sensitive()
