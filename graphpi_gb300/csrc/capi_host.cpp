@@ -227,6 +227,59 @@ int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out) {
         return GPM_ERR_INVALID_ARG;
     }
     p.label_sensitive = plan_label_sensitive(p);
+    // ---- leaf batching of the deepest loop level L (L >= 2) ----
+    p.leaf_kind = kLeafGeneric;
+    p.leaf_fa = p.leaf_fb = p.leaf_sa = p.leaf_sb = -1;
+    p.leaf_ka = p.leaf_kb = 0;
+    p.leaf_cab = p.leaf_cx = 0;
+    // depth at which a prefix is built = its last member = the depth of the chain holding it
+    int built_at[kMaxPrefix];
+    for (int d = 0; d < n; ++d)
+        for (int c = p.chain_begin[d]; c < p.chain_begin[d + 1]; ++c) built_at[p.chain_list[c]] = d;
+    if (p.L >= 2) {
+        if (k == 0) {
+            const int st = p.loop_set[p.T];
+            if (built_at[st] == p.L) {
+                p.leaf_kind = kLeafCount;
+                p.leaf_fa = father[st];  // -1: the set is N(v) itself
+            }
+        } else if (k == 2 && ngroups == 2) {
+            // groups {a}{b} and {a,b} in either order
+            int gab = -1, gx = -1;
+            for (int g = 0; g < 2; ++g) {
+                const int nb = p.group_begin[g + 1] - p.group_begin[g];
+                if (nb == 2) gab = g;
+                if (nb == 1 && p.block_mask[p.group_block[p.group_begin[g]]] == 3u) gx = g;
+            }
+            // every set built at L must be one of the two tail sets
+            bool only_tail_sets = true;
+            for (int c = p.chain_begin[p.L]; c < p.chain_begin[p.L + 1]; ++c)
+                only_tail_sets &= p.chain_list[c] == p.loop_set[p.T] || p.chain_list[c] == p.loop_set[p.T + 1];
+            if (gab >= 0 && gx >= 0 && only_tail_sets) {
+                p.leaf_kind = kLeafIep2;
+                p.leaf_cab = p.group_coef[gab];
+                p.leaf_cx = p.group_coef[gx];
+                p.leaf_sa = p.loop_set[p.T];
+                p.leaf_sb = p.loop_set[p.T + 1];
+                int* kinds[2] = {&p.leaf_ka, &p.leaf_kb};
+                int* probes[2] = {&p.leaf_fa, &p.leaf_fb};
+                const int ids[2] = {p.leaf_sa, p.leaf_sb};
+                for (int q = 0; q < 2; ++q) {
+                    const int sid = ids[q];
+                    if (built_at[sid] < p.L) {
+                        *kinds[q] = 0;  // fixed: probe is the set itself
+                        *probes[q] = sid;
+                    } else if (father[sid] < 0) {
+                        *kinds[q] = 1;  // N(v)
+                        *probes[q] = -1;
+                    } else {
+                        *kinds[q] = 2;  // father ∩ N(v)
+                        *probes[q] = father[sid];
+                    }
+                }
+            }
+        }
+    }
     *out = p;
     return GPM_OK;
 }
@@ -533,7 +586,8 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "chunk") slot = &o.chunk, lo = 1, hi = 1 << 20;
     else if (k == "count_bytes") slot = &o.count_bytes, lo = 0, hi = 1;
     else if (k == "timeout_ms") slot = &o.timeout_ms, lo = 1, hi = 3600 * 1000;
-    else if (k == "stage_max") slot = &o.stage_max, lo = 0, hi = 1 << 16;
+    else if (k == "stage_max") slot = &o.stage_max, lo = 0, hi = 1 << 14;
+    else if (k == "leaf_batch") slot = &o.leaf_batch, lo = 0, hi = 1;
     else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
     else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;
     else if (k == "stripe") slot = &o.stripe, lo = 0, hi = (1 << 30) - 1;
@@ -561,6 +615,7 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "count_bytes") *value = o.count_bytes;
     else if (k == "timeout_ms") *value = o.timeout_ms;
     else if (k == "stage_max") *value = o.stage_max;
+    else if (k == "leaf_batch") *value = o.leaf_batch;
     else if (k == "split") *value = o.split;
     else if (k == "stripes") *value = o.stripes;
     else if (k == "stripe") *value = o.stripe;

@@ -70,6 +70,7 @@ struct WarpState {
     const int* ptr[kMaxPrefix];
     const int* lp[kMaxN];
     int blockval[kMaxBlocks];
+    int leafcnt[3][32];  // per-candidate counters of a leaf batch
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -211,6 +212,12 @@ __device__ __forceinline__ void add128(unsigned long long* o, __int128 v) {
     if (hi + carry) atomicAdd(o + 1, hi + carry);
 }
 
+// x in sorted a[0, n) (per-lane search)
+__device__ __forceinline__ bool contains(const int* __restrict__ a, int n, int x) {
+    const int p = lower_bound_u(a, n, x);
+    return p < n && a[p] == x;
+}
+
 template <bool kBytes>
 struct WarpCtx {
     WarpState* s;
@@ -219,7 +226,181 @@ struct WarpCtx {
     int* scratch;
     int cap;
     int lane;
+    int leaf_on;
+    int* stage;      // 2 * stage_cap ints of this warp's shared memory
+    int stage_cap;
     unsigned long long bytes;
+
+    // copies a fixed set into shared-memory region r when it fits
+    __device__ const int* stage_set(const int* p, int n, int r) {
+        if (n > stage_cap || n <= 0) return p;
+        int* dst = stage + r * stage_cap;
+        for (int i = lane; i < n; i += 32) dst[i] = p[i];
+        __syncwarp();
+        return dst;
+    }
+
+    // Exclusive scan of len over the warp; returns the total.
+    __device__ __forceinline__ int warp_scan(int len, int& pre) const {
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
+        }
+        pre = incl - len;
+        return __shfl_sync(kFull, incl, 31);
+    }
+
+    // owner lane of flat element e: the largest lane c with pre_c <= e
+    __device__ __forceinline__ int owner(int pre, int e) const {
+        int c = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int q = c + step;
+            const int pq = __shfl_sync(kFull, pre, q & 31);
+            if (q < 32 && pq <= e) c = q;
+        }
+        return c;
+    }
+
+    __device__ __forceinline__ bool chosen_before(int x, int L) const {
+        bool hit = false;
+        for (int q = 0; q < L; ++q) hit |= s->chosen[q] == x;
+        return hit;
+    }
+
+    // All candidates of level L at once (the plan's leaf_kind says how the
+    // tail reads N(v)); chosen[0, L) and the level's loop list are set.
+    __device__ __int128 leaf_batch() {
+        const int L = P->L, T = P->T;
+        const int* cand = s->lp[L];
+        const int ncand = s->end[L];
+        long long total = 0;
+        if (P->leaf_kind == kLeafCount) {
+            // bound of the last loop: restrictions on depths < L are fixed
+            const unsigned m = P->rmask[T];
+            int bfix = g.v_cnt;
+            for (int j = 0; j < L; ++j)
+                if (m >> j & 1) bfix = min(bfix, s->chosen[j]);
+            const bool by_v = (m >> L) & 1;
+            const int* F = nullptr;
+            int nf = 0, lim = bfix;
+            if (P->leaf_fa >= 0) {
+                nf = lower_bound_u(s->ptr[P->leaf_fa], s->len[P->leaf_fa], bfix);
+                if (nf == 0) return 0;
+                F = stage_set(s->ptr[P->leaf_fa], nf, 0);
+                lim = min(bfix, F[nf - 1] + 1);
+            }
+            for (int base = 0; base < ncand; base += 32) {
+                const int j = base + lane;
+                bool ok = j < ncand;
+                const int v = ok ? cand[j] : 0;
+                if (ok) ok = !chosen_before(v, L);
+                unsigned st = 0;
+                int len = 0;
+                if (ok) {
+                    st = g.rowptr[v];
+                    const int dv = (int)(g.rowptr[v + 1] - st);
+                    len = lower_bound_u(g.col + st, dv, by_v ? min(lim, v) : lim);
+                    if (kBytes) bytes += 4ull * (unsigned long long)(s->len[P->leaf_fa >= 0 ? P->leaf_fa : 0] * (P->leaf_fa >= 0) + dv) + 8;
+                }
+                int pre;
+                const int M = warp_scan(len, pre);
+                for (int eb = 0; eb < M; eb += 32) {
+                    const int e = eb + lane;
+                    const int c = owner(pre, e);
+                    const unsigned stc = __shfl_sync(kFull, st, c);
+                    const int prc = __shfl_sync(kFull, pre, c);
+                    bool hit = false;
+                    if (e < M) {
+                        const int x = g.col[stc + (e - prc)];
+                        hit = !chosen_before(x, L);
+                        if (hit && F) hit = contains(F, nf, x);
+                    }
+                    total += __popc(__ballot_sync(kFull, hit));
+                }
+            }
+            return lane == 0 ? (__int128)total : (__int128)0;
+        }
+        // ---- two-loop inclusion–exclusion tail ----
+        const int sa = P->leaf_sa, sb = P->leaf_sb, ka = P->leaf_ka, kb = P->leaf_kb;
+        const bool same = sa == sb, both_fixed = ka == 0 && kb == 0;
+        const int* Pa = nullptr;
+        const int* Pb = nullptr;
+        int na = 0, nb = 0;
+        if (P->leaf_fa >= 0) {
+            na = s->len[P->leaf_fa];
+            Pa = stage_set(s->ptr[P->leaf_fa], na, 0);
+        }
+        if (P->leaf_fb >= 0) {
+            nb = s->len[P->leaf_fb];
+            Pb = (P->leaf_fb == P->leaf_fa) ? Pa : stage_set(s->ptr[P->leaf_fb], nb, 1);
+        }
+        const int fixA = ka == 0 ? count_outside(s->ptr[sa], s->len[sa], s->chosen, L, lane) : 0;
+        const int fixB = kb == 0 ? count_outside(s->ptr[sb], s->len[sb], s->chosen, L, lane) : 0;
+        const int fixX = (both_fixed && !same)
+                             ? isect_count(s->ptr[sa], s->len[sa], s->ptr[sb], s->len[sb], INT_MAX, s->chosen, L, lane)
+                             : 0;
+        const long long cab = P->leaf_cab, cx = P->leaf_cx;
+        for (int base = 0; base < ncand; base += 32) {
+            const int j = base + lane;
+            bool ok = j < ncand;
+            const int v = ok ? cand[j] : 0;
+            if (ok) ok = !chosen_before(v, L);
+            unsigned st = 0;
+            int len = 0;
+            bool inA = false, inB = false;
+            if (ok) {
+                if (ka == 0) inA = contains(Pa, na, v);
+                if (kb == 0) inB = contains(Pb, nb, v);
+                if (!both_fixed) {
+                    st = g.rowptr[v];
+                    len = (int)(g.rowptr[v + 1] - st);
+                }
+            }
+            s->leafcnt[0][lane] = 0;
+            s->leafcnt[1][lane] = 0;
+            s->leafcnt[2][lane] = 0;
+            __syncwarp();
+            int pre;
+            const int M = warp_scan(len, pre);
+            for (int eb = 0; eb < M; eb += 32) {
+                const int e = eb + lane;
+                const int c = owner(pre, e);
+                const unsigned stc = __shfl_sync(kFull, st, c);
+                const int prc = __shfl_sync(kFull, pre, c);
+                bool ma = false, mb = false;
+                if (e < M) {
+                    const int x = g.col[stc + (e - prc)];
+                    if (!chosen_before(x, L)) {
+                        ma = ka == 1 ? true : contains(Pa, na, x);
+                        mb = kb == 1 ? true : contains(Pb, nb, x);
+                    }
+                }
+                const unsigned grp = __match_any_sync(kFull, e < M ? c : 32 + lane);
+                const unsigned ba = __ballot_sync(kFull, ma), bb = __ballot_sync(kFull, mb),
+                               bx = __ballot_sync(kFull, ma && mb);
+                if (e < M && lane == __ffs(grp) - 1) {
+                    s->leafcnt[0][c] += __popc(ba & grp);
+                    s->leafcnt[1][c] += __popc(bb & grp);
+                    s->leafcnt[2][c] += __popc(bx & grp);
+                }
+                __syncwarp();
+            }
+            if (ok) {
+                const long long A = ka == 0 ? (long long)(fixA - (inA ? 1 : 0)) : s->leafcnt[0][lane];
+                const long long B = kb == 0 ? (long long)(fixB - (inB ? 1 : 0)) : s->leafcnt[1][lane];
+                const long long X = same ? A : (both_fixed ? (long long)(fixX - (inA && inB ? 1 : 0)) : s->leafcnt[2][lane]);
+                total += cab * A * B + cx * X;
+                if (kBytes) bytes += 4ull * (unsigned long long)(len + (ka == 2 ? na : 0) + (kb == 2 ? nb : 0) + A + B) + 8;
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(kFull, total, o);
+        return lane == 0 ? (__int128)total : (__int128)0;
+    }
 
     __device__ __forceinline__ void nbr(int v, const int*& p, int& d) const {
         const unsigned a = g.rowptr[v], b = g.rowptr[v + 1];
@@ -369,9 +550,11 @@ struct WarpCtx {
     // levels 2..L below a fixed (v0, v1)
     __device__ __int128 dfs_from_2() {
         const int L = P->L;
+        const bool batch = leaf_on && P->leaf_kind != kLeafGeneric;
         __int128 acc = 0;
         int d = 2;
         start_level(2);
+        if (batch && L == 2) return leaf_batch();
         while (d >= 2) {
             const int i = s->idx[d];
             if (i >= s->end[d]) {
@@ -395,6 +578,10 @@ struct WarpCtx {
             set_chosen(d, v);
             ++d;
             start_level(d);
+            if (batch && d == L) {
+                acc += leaf_batch();
+                --d;
+            }
         }
         return acc;
     }
@@ -428,17 +615,22 @@ struct WarpCtx {
 };
 
 template <bool kBytes>
-__global__ void __launch_bounds__(512) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
+__global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
                                                     unsigned long long* __restrict__ cursors,
                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
                                                     long long scratch_per_warp, int chunk,
                                                     unsigned long long stripes, unsigned long long stripe,
+                                                    int leaf_on, int stage_cap,
                                                     unsigned long long* __restrict__ stats) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wid;
+    const int nwarps = blockDim.x >> 5;
+    const long long gw = (long long)blockIdx.x * nwarps + wid;
     WarpCtx<kBytes> w;
     w.s = reinterpret_cast<WarpState*>(smem_raw) + wid;
+    w.stage = reinterpret_cast<int*>(reinterpret_cast<WarpState*>(smem_raw) + nwarps) + (size_t)wid * 2 * stage_cap;
+    w.stage_cap = stage_cap;
+    w.leaf_on = leaf_on;
     w.scratch = scratch_all + gw * scratch_per_warp;
     w.lane = lane;
     w.bytes = 0;
@@ -781,16 +973,21 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     cudaStream_t st = c->stream;
     GPM_CK(cudaMemcpyAsync(d_pairs.p, descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
     GPM_CK(cudaMemsetAsync(d_small.p, 0, small_words * sizeof(unsigned long long), st));
-    const size_t smem = sizeof(WarpState) * wpb;
+    const int stage_cap = (int)o.stage_max;
+    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
+    if (o.count_bytes)
+        GPM_CK(cudaFuncSetAttribute(match_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    else
+        GPM_CK(cudaFuncSetAttribute(match_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     GPM_CK(cudaEventRecord(c->ev0, st));
     if (o.count_bytes)
         match_kernel<true><<<(unsigned)blocks, wpb * 32, smem, st>>>(
             (const PairDesc*)d_pairs.p, n, cursors, out, (int*)c->scratch, per_warp, (int)o.chunk,
-            (unsigned long long)o.stripes, (unsigned long long)o.stripe, stats);
+            (unsigned long long)o.stripes, (unsigned long long)o.stripe, (int)o.leaf_batch, stage_cap, stats);
     else
         match_kernel<false><<<(unsigned)blocks, wpb * 32, smem, st>>>(
             (const PairDesc*)d_pairs.p, n, cursors, out, (int*)c->scratch, per_warp, (int)o.chunk,
-            (unsigned long long)o.stripes, (unsigned long long)o.stripe, stats);
+            (unsigned long long)o.stripes, (unsigned long long)o.stripe, (int)o.leaf_batch, stage_cap, stats);
     GPM_CK(cudaGetLastError());
     GPM_CK(cudaEventRecord(c->ev1, st));
     std::vector<unsigned long long> raw(2 * n + 2);

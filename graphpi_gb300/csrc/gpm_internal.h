@@ -20,7 +20,8 @@ struct Options {
     int64_t chunk = 8;          // first-level tasks per queue grab
     int64_t count_bytes = 0;    // 1: count algorithmic bytes
     int64_t timeout_ms = 2000;  // bounded device waits
-    int64_t stage_max = 0;      // reserved: father sets staged in shared memory
+    int64_t stage_max = 1024;   // largest fixed set staged in shared memory (ints)
+    int64_t leaf_batch = 1;     // 1: batched deepest level where the plan allows
     int64_t split = 0;          // reserved: hub splitting width
     int64_t stripes = 1;        // a launch covers chunks q*stripes + stripe only
     int64_t stripe = 0;
@@ -46,6 +47,18 @@ struct DevPlan {
     int nblocks;
     int ngroups;
     int label_sensitive;  // 1: the count depends on vertex labels; run on the caller's ids
+    // Batched evaluation of the deepest loop level L (all candidates of a
+    // level at once, one flat lane-balanced scan over their neighbour lists):
+    //   kLeafGeneric  candidate by candidate (build_chain + tail)
+    //   kLeafCount    no tail: count N(v) elements below the bound, outside
+    //                 the chosen vertices and (leaf_fa >= 0) inside set leaf_fa
+    //   kLeafIep2     two-loop inclusion–exclusion tail; sets a/b are
+    //                 fixed (built before L), N(v), or father ∩ N(v)
+    int leaf_kind;
+    int leaf_fa, leaf_fb;        // probe prefix of set a / b (-1: none)
+    int leaf_sa, leaf_sb;        // prefix ids of the tail's loop sets (kLeafIep2)
+    int leaf_ka, leaf_kb;        // 0 fixed, 1 N(v), 2 father ∩ N(v)
+    int leaf_cab, leaf_cx;       // group coefficients of |a|*|b| and |a ∩ b|
     long long redundancy;
     int loop_set[kMaxN];
     unsigned rmask[kMaxN];         // depth d stays below min(chosen[j]) for bits j
@@ -58,6 +71,8 @@ struct DevPlan {
     int group_coef[kMaxGroups];
     unsigned char group_block[kMaxGroupEntries];
 };
+
+constexpr int kLeafGeneric = 0, kLeafCount = 1, kLeafIep2 = 2;
 
 // Decodes gpm_schedule_build tables into a DevPlan (host).
 int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out);
