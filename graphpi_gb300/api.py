@@ -345,6 +345,40 @@ def batch_count(graphs: list[Graph], schedules: list[Schedule]) -> list[int]:
             p.close()
 
 
+class BatchExec:
+    """A batched launch captured once in a CUDA graph and replayed
+    (gpm_batch_exec_run).  Options in force at the first run (grid, chunk,
+    staging) are baked in; the stripe options are read at every replay."""
+
+    def __init__(self, graphs: list[Graph], schedules: list[Schedule]):
+        if len(graphs) != len(schedules):
+            raise ValueError("graphs and schedules differ in length")
+        self.graphs = graphs
+        self.plans = [Plan(s) for s in schedules]
+        self.n = len(self.plans)
+        self._gh = (C.c_void_p * self.n)(*[g.device() for g in graphs])
+        self._ph = (C.c_void_p * self.n)(*[p.handle for p in self.plans])
+        self._exec = C.c_void_p()
+
+    def run(self) -> list[int]:
+        outs = (U128 * self.n)()
+        check(lib().gpm_batch_exec_run(C.byref(self._exec), self.n, self._gh, self._ph, outs), "gpm_batch_exec_run")
+        return [o.value for o in outs]
+
+    def close(self) -> None:
+        if self._exec:
+            lib().gpm_batch_exec_destroy(self._exec)
+            self._exec = C.c_void_p()
+        for p in self.plans:
+            p.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def count_host(graph: Graph, schedules: list[Schedule]) -> list[int]:
     """One-shot host-buffer path (gpm_count_host): upload, relabel, batched
     count, download, free."""

@@ -619,9 +619,12 @@ __global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restric
                                                     unsigned long long* __restrict__ cursors,
                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
                                                     long long scratch_per_warp, int chunk,
-                                                    unsigned long long stripes, unsigned long long stripe,
+                                                    const unsigned long long* __restrict__ params,
                                                     int leaf_on, int stage_cap,
                                                     unsigned long long* __restrict__ stats) {
+    // params[0] = stripes, params[1] = stripe (device memory, so a captured
+    // graph can replay with new values)
+    const unsigned long long stripes = params[0], stripe = params[1];
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -925,13 +928,24 @@ static GraphView view_of(const gpm_graph* g, bool caller_ids = false) {
     return v;
 }
 
-// Launches the matcher over n pairs and leaves raw 128-bit sums in host_raw
-// (2 words per pair).
-static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_plan* const* plans,
-                     unsigned long long* host_raw) {
+struct LaunchSetup {
+    std::vector<PairDesc> descs;
+    long long blocks = 0;
+    int wpb = 0;
+    long long per_warp = 0;
+    int stage_cap = 0;
+    size_t smem = 0;
+    int chunk = 0;
+    int leaf_on = 0;
+    bool count_bytes = false;
+};
+
+// Validates the pairs and sizes the launch from the current options.
+static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_plan* const* plans,
+                         size_t scratch_budget_extra, LaunchSetup& ls) {
     Options& o = options();
     int cap = 1, nslots = 1;
-    std::vector<PairDesc> descs(n);
+    ls.descs.assign(n, PairDesc());
     for (int i = 0; i < n; ++i) {
         const gpm_graph* g = graphs[i];
         const gpm_plan* p = plans[i];
@@ -943,55 +957,81 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
             set_error("pair %d: graph/plan live on another device", i);
             return GPM_ERR_INVALID_ARG;
         }
-        descs[i].g = view_of(g, p->host.label_sensitive != 0);
-        descs[i].plan = p->dev;
-        descs[i].ntasks = p->host.T == 1 ? (unsigned long long)g->v_cnt : (unsigned long long)g->e_cnt;
+        PairDesc& d = ls.descs[i];
+        d.g = view_of(g, p->host.label_sensitive != 0);
+        d.plan = p->dev;
+        d.ntasks = p->host.T == 1 ? (unsigned long long)g->v_cnt : (unsigned long long)g->e_cnt;
         // every set built is a subset of one neighbour list: the largest degree
         // bounds it (inclusion-exclusion temporaries can be N(v0) itself)
-        descs[i].cap = std::max(1, g->max_degree);
-        descs[i].pad_ = 0;
-        cap = std::max(cap, descs[i].cap);
+        d.cap = std::max(1, g->max_degree);
+        d.pad_ = 0;
+        cap = std::max(cap, d.cap);
         nslots = std::max(nslots, p->host.nslots);
     }
-    const int wpb = (int)o.warps_per_block;
-    long long blocks = (long long)c->num_sms * o.blocks_per_sm;
-    const long long per_warp = (long long)nslots * cap;
+    ls.wpb = (int)o.warps_per_block;
+    ls.blocks = (long long)c->num_sms * o.blocks_per_sm;
+    ls.per_warp = (long long)nslots * cap;
     // shrink the grid when the per-warp scratch would not fit in free memory
     size_t free_b = 0, total_b = 0;
     GPM_CK(cudaMemGetInfo(&free_b, &total_b));
-    const size_t budget = (size_t)((free_b + c->scratch_bytes) * 0.6);
-    while (blocks > 1 && (size_t)blocks * wpb * per_warp * sizeof(int) > budget) blocks = (blocks + 1) / 2;
-    int rc = ensure_scratch(c, (size_t)blocks * wpb * per_warp * sizeof(int));
+    const size_t budget = (size_t)((free_b + scratch_budget_extra) * 0.6);
+    while (ls.blocks > 1 && (size_t)ls.blocks * ls.wpb * ls.per_warp * sizeof(int) > budget)
+        ls.blocks = (ls.blocks + 1) / 2;
+    ls.stage_cap = (int)o.stage_max;
+    ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)ls.stage_cap * ls.wpb;
+    ls.chunk = (int)o.chunk;
+    ls.leaf_on = (int)o.leaf_batch;
+    ls.count_bytes = o.count_bytes != 0;
+    if (ls.count_bytes)
+        GPM_CK(cudaFuncSetAttribute(match_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
+    else
+        GPM_CK(cudaFuncSetAttribute(match_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
+    return GPM_OK;
+}
+
+// small device words of a launch: cursors[n], out[2n], stats[2], params[2]
+static size_t small_words(int n) { return (size_t)n * 3 + 4; }
+
+static void enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d_pairs, unsigned long long* d_small,
+                          int* scratch, cudaStream_t st) {
+    unsigned long long* cursors = d_small;
+    unsigned long long* out = cursors + n;
+    unsigned long long* stats = out + 2 * n;
+    const unsigned long long* params = stats + 2;
+    if (ls.count_bytes)
+        match_kernel<true><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
+            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, stats);
+    else
+        match_kernel<false><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
+            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, stats);
+}
+
+// Launches the matcher over n pairs and leaves raw 128-bit sums in host_raw
+// (2 words per pair).
+static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_plan* const* plans,
+                     unsigned long long* host_raw) {
+    LaunchSetup ls;
+    int rc = prepare_pairs(c, n, graphs, plans, c->scratch_bytes, ls);
+    if (rc) return rc;
+    rc = ensure_scratch(c, (size_t)ls.blocks * ls.wpb * ls.per_warp * sizeof(int));
     if (rc) return rc;
     DevBuf d_pairs, d_small;
     GPM_CK(cudaMalloc(&d_pairs.p, sizeof(PairDesc) * n));
-    const size_t small_words = (size_t)n + 2 * (size_t)n + 2;  // cursors, out, stats
-    GPM_CK(cudaMalloc(&d_small.p, small_words * sizeof(unsigned long long)));
-    unsigned long long* cursors = (unsigned long long*)d_small.p;
-    unsigned long long* out = cursors + n;
-    unsigned long long* stats = out + 2 * n;
+    const size_t words = small_words(n);
+    GPM_CK(cudaMalloc(&d_small.p, words * sizeof(unsigned long long)));
     cudaStream_t st = c->stream;
-    GPM_CK(cudaMemcpyAsync(d_pairs.p, descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
-    GPM_CK(cudaMemsetAsync(d_small.p, 0, small_words * sizeof(unsigned long long), st));
-    const int stage_cap = (int)o.stage_max;
-    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
-    if (o.count_bytes)
-        GPM_CK(cudaFuncSetAttribute(match_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    else
-        GPM_CK(cudaFuncSetAttribute(match_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    std::vector<unsigned long long> init(words, 0);
+    init[3 * n + 2] = (unsigned long long)options().stripes;
+    init[3 * n + 3] = (unsigned long long)options().stripe;
+    GPM_CK(cudaMemcpyAsync(d_pairs.p, ls.descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
+    GPM_CK(cudaMemcpyAsync(d_small.p, init.data(), words * sizeof(unsigned long long), cudaMemcpyHostToDevice, st));
     GPM_CK(cudaEventRecord(c->ev0, st));
-    if (o.count_bytes)
-        match_kernel<true><<<(unsigned)blocks, wpb * 32, smem, st>>>(
-            (const PairDesc*)d_pairs.p, n, cursors, out, (int*)c->scratch, per_warp, (int)o.chunk,
-            (unsigned long long)o.stripes, (unsigned long long)o.stripe, (int)o.leaf_batch, stage_cap, stats);
-    else
-        match_kernel<false><<<(unsigned)blocks, wpb * 32, smem, st>>>(
-            (const PairDesc*)d_pairs.p, n, cursors, out, (int*)c->scratch, per_warp, (int)o.chunk,
-            (unsigned long long)o.stripes, (unsigned long long)o.stripe, (int)o.leaf_batch, stage_cap, stats);
+    enqueue_match(ls, n, (const PairDesc*)d_pairs.p, (unsigned long long*)d_small.p, (int*)c->scratch, st);
     GPM_CK(cudaGetLastError());
     GPM_CK(cudaEventRecord(c->ev1, st));
     std::vector<unsigned long long> raw(2 * n + 2);
-    GPM_CK(cudaMemcpyAsync(raw.data(), out, sizeof(unsigned long long) * (2 * n + 2), cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaMemcpyAsync(raw.data(), (unsigned long long*)d_small.p + n, sizeof(unsigned long long) * (2 * n + 2),
+                           cudaMemcpyDeviceToHost, st));
     GPM_CK(cudaStreamSynchronize(st));
     float ms = 0;
     GPM_CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
@@ -1256,22 +1296,102 @@ GPM_API int gpm_count_host(int32_t v_cnt, const uint32_t* rowptr, const int32_t*
 struct gpm_batch_exec {
     int n = 0;
     int device = 0;
-    std::vector<gpm_graph*> graphs;
     std::vector<const gpm_plan*> plans;
+    LaunchSetup ls;
+    void* d_pairs = nullptr;
+    unsigned long long* d_small = nullptr;
+    unsigned long long* h_small = nullptr;  // pinned: out[2n], stats[2], params[2]
+    int* scratch = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~gpm_batch_exec() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (d_pairs) cudaFree(d_pairs);
+        if (d_small) cudaFree(d_small);
+        if (h_small) cudaFreeHost(h_small);
+        if (scratch) cudaFree(scratch);
+    }
 };
+
+// Builds the replayable graph: params H2D, zero the counters, the
+// persistent launch, results D2H.  The exec owns its buffers so other calls
+// cannot move them between replays.
+static int exec_build(DeviceCtx* c, gpm_batch_exec* e, gpm_graph* const* graphs) {
+    const int n = e->n;
+    int rc = prepare_pairs(c, n, graphs, e->plans.data(), 0, e->ls);
+    if (rc) return rc;
+    const size_t words = small_words(n);
+    GPM_CK(cudaMalloc(&e->d_pairs, sizeof(PairDesc) * n));
+    GPM_CK(cudaMalloc(&e->d_small, words * sizeof(unsigned long long)));
+    GPM_CK(cudaMallocHost(&e->h_small, (2 * (size_t)n + 4) * sizeof(unsigned long long)));
+    GPM_CK(cudaMalloc(&e->scratch, std::max<size_t>(1, (size_t)e->ls.blocks * e->ls.wpb * e->ls.per_warp * sizeof(int))));
+    cudaStream_t st = c->stream;
+    GPM_CK(cudaMemcpyAsync(e->d_pairs, e->ls.descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    unsigned long long* h_params = e->h_small + 2 * n + 2;
+    unsigned long long* d_params = e->d_small + 3 * n + 2;
+    GPM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaMemcpyAsync(d_params, h_params, 2 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(e->d_small, 0, (3 * (size_t)n + 2) * sizeof(unsigned long long), st);
+    enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, st);
+    cudaMemcpyAsync(e->h_small, e->d_small + n, (2 * (size_t)n + 2) * sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost, st);
+    cudaGraph_t g = nullptr;
+    cudaError_t err = cudaStreamEndCapture(st, &g);
+    if (err != cudaSuccess) {
+        set_error("CUDA graph capture failed: %s", cudaGetErrorString(err));
+        if (g) cudaGraphDestroy(g);
+        return GPM_ERR_CUDA;
+    }
+    e->graph = g;
+    GPM_CK(cudaGraphInstantiate(&e->exec, g, 0));
+    return GPM_OK;
+}
 
 GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph* const* graphs,
                                const gpm_plan* const* plans, gpm_u128* outs) {
     clear_error();
-    if (!exec) return GPM_ERR_INVALID_ARG;
+    if (!exec || n_pairs < 1 || !graphs || !plans || !outs) {
+        set_error("gpm_batch_exec_run: need n_pairs >= 1 and non-null arrays");
+        return GPM_ERR_INVALID_ARG;
+    }
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> lk(c->mu);
     if (!*exec) {
         gpm_batch_exec* e = new gpm_batch_exec();
         e->n = n_pairs;
-        e->graphs.assign(graphs, graphs + n_pairs);
+        e->device = c->device;
         e->plans.assign(plans, plans + n_pairs);
+        int rc = exec_build(c, e, graphs);
+        if (rc) {
+            delete e;
+            return rc;
+        }
         *exec = e;
     }
-    return gpm_batch_count((*exec)->n, (*exec)->graphs.data(), (*exec)->plans.data(), outs);
+    gpm_batch_exec* e = *exec;
+    if (e->n != n_pairs || e->device != c->device) {
+        set_error("gpm_batch_exec_run: exec was built for %d pairs on device %d", e->n, e->device);
+        return GPM_ERR_INVALID_ARG;
+    }
+    const int n = e->n;
+    e->h_small[2 * n + 2] = (unsigned long long)options().stripes;
+    e->h_small[2 * n + 3] = (unsigned long long)options().stripe;
+    cudaStream_t st = c->stream;
+    GPM_CK(cudaEventRecord(c->ev0, st));
+    GPM_CK(cudaGraphLaunch(e->exec, st));
+    GPM_CK(cudaEventRecord(c->ev1, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    GPM_CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    t_ms = ms;
+    t_launches = 1;
+    t_bytes = e->h_small[2 * n];
+    std::vector<unsigned long long> raw(e->h_small, e->h_small + 2 * n);
+    return finish_counts(n, e->plans.data(), raw.data(), outs);
 }
 
 GPM_API int gpm_batch_exec_destroy(gpm_batch_exec* exec) {

@@ -185,3 +185,51 @@ def test_engine_knobs_do_not_change_counts(engine, oracle):
         finally:
             for k, v in old.items():
                 gp.set_option(k, v)
+
+
+def test_cuda_graph_replay_matches_batch(engine, oracle):
+    g = gp.rmat(11, 10, 0.57, 0.19, 0.19, 8)
+    tri = g.triangle_counting_mt()
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
+    want = gp.batch_count([g] * len(scheds), scheds)
+    ex = gp.BatchExec([g] * len(scheds), scheds)
+    try:
+        assert ex.run() == want
+        assert ex.run() == want  # replay
+        # replays over stripes sum to the whole job
+        gp.set_option("raw_sums", 1)
+        gp.set_option("stripes", 4)
+        tot = [0] * len(scheds)
+        for st in range(4):
+            gp.set_option("stripe", st)
+            for i, r in enumerate(ex.run()):
+                tot[i] += r - (1 << 128) if r >= (1 << 127) else r
+        red = [s.get_in_exclusion_optimize_redundancy() for s in scheds]
+        assert [t // d for t, d in zip(tot, red)] == want
+    finally:
+        gp.set_option("stripes", 1)
+        gp.set_option("stripe", 0)
+        gp.set_option("raw_sums", 0)
+        ex.close()
+
+
+def test_leaf_batch_matches_per_candidate_path(engine, oracle):
+    g = gp.chung_lu(3000, 14.0, 2.2, 400, 41)
+    tri = g.triangle_counting_mt()
+    for flags in [(1, 1, True), (1, 1, False), (0, 1, True)]:
+        scheds = [gp.Schedule(p, flags[0], flags[1], flags[2], g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
+        scheds = [s for s in scheds if s.is_pattern_valid]
+        batched = gp.batch_count([g] * len(scheds), scheds)
+        gp.set_option("leaf_batch", 0)
+        try:
+            plain = gp.batch_count([g] * len(scheds), scheds)
+        finally:
+            gp.set_option("leaf_batch", 1)
+        assert batched == plain == [oracle.count(g, s) for s in scheds]
+    # tiny staging area forces the global-memory probe path
+    old = gp.get_option("stage_max")
+    gp.set_option("stage_max", 16)
+    try:
+        assert gp.batch_count([g] * len(scheds), scheds) == batched
+    finally:
+        gp.set_option("stage_max", old)
