@@ -6,11 +6,11 @@ reference's Graph / Pattern / Schedule / DataLoader / MotifGenerator API.
 """
 from .api import (BatchExec, DataLoader, DataType, Graph, MotifGenerator, Pattern, PatternType, Plan, Schedule,
                   batch_count, chung_lu, complete_graph, count_host, from_edges, motifs_3_to_5, relabel_by_degree,
-                  rmat)
+                  rmat, schedule_candidates, schedule_from_order)
 from .native import GpmError, get_option, last_launch_stats, lib, set_option
 
 __all__ = [
     "BatchExec", "DataLoader", "DataType", "Graph", "MotifGenerator", "Pattern", "PatternType", "Plan", "Schedule",
     "batch_count", "chung_lu", "complete_graph", "count_host", "from_edges", "motifs_3_to_5",
-    "relabel_by_degree", "rmat", "GpmError", "get_option", "last_launch_stats", "lib", "set_option",
+    "relabel_by_degree", "rmat", "schedule_candidates", "schedule_from_order", "GpmError", "get_option", "last_launch_stats", "lib", "set_option",
 ]

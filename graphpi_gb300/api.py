@@ -232,6 +232,53 @@ class Schedule:
     def get_adj_mat_ptr(self): return self.adj_mat.reshape(-1)
 
 
+MAX_PAIRS = 28
+
+
+def schedule_candidates(pattern: "Pattern", performance_modeling_type: int, restricts_type: int, v_cnt: int,
+                        e_cnt: int, tri_cnt: int) -> list[dict]:
+    """Every (loop order, restriction set) the Schedule constructor scores,
+    with its analytic cost (gpm_schedule_candidates)."""
+    n = pattern.get_size()
+    a = np.ascontiguousarray(pattern.adj, dtype=np.int32)
+    cnt = C.c_int32()
+    check(lib().gpm_schedule_candidates(n, a.ctypes.data, performance_modeling_type, restricts_type, v_cnt, e_cnt,
+                                        tri_cnt, None, None, None, None, 0, C.byref(cnt)), "candidates")
+    k = cnt.value
+    orders = np.zeros(k * n, dtype=np.int32)
+    npairs = np.zeros(k, dtype=np.int32)
+    pairs = np.zeros(k * 2 * MAX_PAIRS, dtype=np.int32)
+    costs = np.zeros(k, dtype=np.float64)
+    check(lib().gpm_schedule_candidates(n, a.ctypes.data, performance_modeling_type, restricts_type, v_cnt, e_cnt,
+                                        tri_cnt, orders.ctypes.data, npairs.ctypes.data, pairs.ctypes.data,
+                                        costs.ctypes.data, k, C.byref(cnt)), "candidates")
+    out = []
+    for i in range(k):
+        pr = pairs[i * 2 * MAX_PAIRS: i * 2 * MAX_PAIRS + 2 * npairs[i]].reshape(-1, 2)
+        out.append({"order": orders[i * n:(i + 1) * n].tolist(), "pairs": [tuple(map(int, x)) for x in pr],
+                    "cost": float(costs[i])})
+    return out
+
+
+def schedule_from_order(pattern: "Pattern", order, pairs, use_in_exclusion_optimize: bool = True,
+                        restricts_type: int = 1) -> "Schedule":
+    """The schedule for one candidate (gpm_schedule_from_order)."""
+    n = pattern.get_size()
+    a = np.ascontiguousarray(pattern.adj, dtype=np.int32)
+    o = np.ascontiguousarray(order, dtype=np.int32)
+    pr = np.ascontiguousarray(np.array(pairs, dtype=np.int32).reshape(-1))
+    buf = np.zeros(8192, dtype=np.int64)
+    nw, valid = C.c_int32(), C.c_int32()
+    check(lib().gpm_schedule_from_order(n, a.ctypes.data, o.ctypes.data, len(pr) // 2, pr.ctypes.data if len(pr) else None,
+                                        1 if use_in_exclusion_optimize else 0, restricts_type, buf.ctypes.data,
+                                        len(buf), C.byref(nw), C.byref(valid)), "schedule_from_order")
+    if not valid.value:
+        raise ValueError("order is not prefix-connected")
+    s = Schedule.from_tables(buf[:nw.value])
+    s.pattern = pattern
+    return s
+
+
 class Plan:
     """A schedule compiled for the device (gpm_plan)."""
 

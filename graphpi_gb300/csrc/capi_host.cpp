@@ -564,6 +564,78 @@ GPM_API int gpm_schedule_build(int32_t n, const int32_t* adj, int32_t perf_type,
     }
 }
 
+GPM_API int gpm_schedule_candidates(int32_t n, const int32_t* adj, int32_t perf_type, int32_t restricts_type,
+                                    int64_t v_cnt, uint64_t e_cnt, int64_t tri_cnt, int32_t* orders,
+                                    int32_t* n_pairs, int32_t* pairs, double* costs, int32_t cap,
+                                    int32_t* count) {
+    gpm::clear_error();
+    if (n < 2 || n > gpm::kMaxN || !adj || !count || cap < 0 || (cap > 0 && (!orders || !n_pairs || !pairs || !costs))) {
+        set_error("gpm_schedule_candidates: bad arguments");
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (perf_type < 1 || perf_type > 3 || restricts_type < 0 || restricts_type > 2 || v_cnt < 1 || e_cnt == 0 ||
+        e_cnt > UINT32_MAX || (perf_type == 1 && tri_cnt < 0)) {
+        set_error("gpm_schedule_candidates: perf_type must be 1..3 with valid graph statistics");
+        return GPM_ERR_INVALID_ARG;
+    }
+    try {
+        Pattern p(n);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j)
+                if (adj[i * n + j] && i != j) p.add_edge(i, j);
+        auto cands = Schedule::candidates(p, perf_type, restricts_type, (int)v_cnt, (unsigned)e_cnt, tri_cnt);
+        *count = (int32_t)cands.size();
+        for (int c = 0; c < (int)cands.size() && c < cap; ++c) {
+            for (int j = 0; j < n; ++j) orders[c * n + j] = cands[c].order[j];
+            const int np = std::min<int>((int)cands[c].pairs.size(), GPM_MAX_PAIRS);
+            n_pairs[c] = np;
+            for (int q = 0; q < np; ++q) {
+                pairs[(size_t)c * 2 * GPM_MAX_PAIRS + 2 * q] = cands[c].pairs[q].first;
+                pairs[(size_t)c * 2 * GPM_MAX_PAIRS + 2 * q + 1] = cands[c].pairs[q].second;
+            }
+            costs[c] = cands[c].cost;
+        }
+        return GPM_OK;
+    } catch (const std::exception& e) {
+        set_error("gpm_schedule_candidates: %s", e.what());
+        return GPM_ERR_INVALID_ARG;
+    }
+}
+
+GPM_API int gpm_schedule_from_order(int32_t n, const int32_t* adj, const int32_t* order, int32_t n_pairs,
+                                    const int32_t* pairs, int32_t use_iep, int32_t restricts_type, int64_t* tables,
+                                    int32_t cap, int32_t* n_words, int32_t* valid) {
+    gpm::clear_error();
+    if (n < 2 || n > gpm::kMaxN || !adj || !order || n_pairs < 0 || n_pairs > GPM_MAX_PAIRS ||
+        (n_pairs > 0 && !pairs) || !n_words || !valid) {
+        set_error("gpm_schedule_from_order: bad arguments");
+        return GPM_ERR_INVALID_ARG;
+    }
+    try {
+        Pattern p(n);
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j)
+                if (adj[i * n + j] && i != j) p.add_edge(i, j);
+        std::vector<int> ord(order, order + n);
+        std::vector<std::pair<int, int> > pr;
+        for (int q = 0; q < n_pairs; ++q) pr.push_back(std::make_pair(pairs[2 * q], pairs[2 * q + 1]));
+        bool ok = false;
+        Schedule s(p, ord, pr, use_iep != 0, restricts_type, ok);
+        *valid = ok ? 1 : 0;
+        std::vector<int64_t> t = ok ? s.pack() : std::vector<int64_t>();
+        *n_words = (int32_t)t.size();
+        if ((int32_t)t.size() > cap || (!tables && !t.empty())) {
+            set_error("gpm_schedule_from_order: output needs %d words, capacity %d", (int)t.size(), cap);
+            return GPM_ERR_INVALID_ARG;
+        }
+        if (!t.empty()) memcpy(tables, t.data(), t.size() * sizeof(int64_t));
+        return GPM_OK;
+    } catch (const std::exception& e) {
+        set_error("gpm_schedule_from_order: %s", e.what());
+        return GPM_ERR_INVALID_ARG;
+    }
+}
+
 GPM_API int gpm_schedule_analyze(const int64_t* tables, int32_t n_words, int32_t* label_sensitive) {
     gpm::clear_error();
     if (!label_sensitive) return GPM_ERR_INVALID_ARG;
@@ -592,6 +664,9 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;
     else if (k == "stripe") slot = &o.stripe, lo = 0, hi = (1 << 30) - 1;
     else if (k == "raw_sums") slot = &o.raw_sums, lo = 0, hi = 1;
+    else if (k == "merge_alpha4_small") slot = &o.merge_alpha4[0], lo = 0, hi = 1024;
+    else if (k == "merge_alpha4_mid") slot = &o.merge_alpha4[1], lo = 0, hi = 1024;
+    else if (k == "merge_alpha4_large") slot = &o.merge_alpha4[2], lo = 0, hi = 1024;
     if (!slot) {
         set_error("gpm_set_option: unknown key '%s'", key);
         return GPM_ERR_INVALID_ARG;
@@ -620,6 +695,9 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "stripes") *value = o.stripes;
     else if (k == "stripe") *value = o.stripe;
     else if (k == "raw_sums") *value = o.raw_sums;
+    else if (k == "merge_alpha4_small") *value = o.merge_alpha4[0];
+    else if (k == "merge_alpha4_mid") *value = o.merge_alpha4[1];
+    else if (k == "merge_alpha4_large") *value = o.merge_alpha4[2];
     else {
         set_error("gpm_get_option: unknown key '%s'", key);
         return GPM_ERR_INVALID_ARG;

@@ -127,9 +127,14 @@ __device__ int warp_merge(const int* __restrict__ A, int na, const int* __restri
 // Merge when both lists are of similar length: a binary-search round costs
 // about log2(nb) dependent loads for 32 elements of the short list, a merge
 // step one coalesced load per list for at least 32 elements.
+// alpha4 = 4 x the weight of a binary-search round, per bucket of the longer
+// list's length (< 256, < 8192, larger); the autotuner sets them.
+__constant__ int c_merge_alpha4[3] = {4, 4, 4};
+
 __device__ __forceinline__ bool prefer_merge(int na, int nb) {
     const int lg = 32 - __clz(nb | 1);
-    return (long long)na * lg >= (long long)(na + nb);
+    const int a4 = c_merge_alpha4[nb < 256 ? 0 : (nb < 8192 ? 1 : 2)];
+    return (long long)na * lg * a4 >= 4ll * (long long)(na + nb);
 }
 
 // A ∩ B written sorted to out; returns its size.
@@ -977,6 +982,8 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
     const size_t budget = (size_t)((free_b + scratch_budget_extra) * 0.6);
     while (ls.blocks > 1 && (size_t)ls.blocks * ls.wpb * ls.per_warp * sizeof(int) > budget)
         ls.blocks = (ls.blocks + 1) / 2;
+    const int alpha4[3] = {(int)o.merge_alpha4[0], (int)o.merge_alpha4[1], (int)o.merge_alpha4[2]};
+    GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, c->stream));
     ls.stage_cap = (int)o.stage_max;
     ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)ls.stage_cap * ls.wpb;
     ls.chunk = (int)o.chunk;

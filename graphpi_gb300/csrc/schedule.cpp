@@ -309,6 +309,80 @@ Schedule::Schedule(const Pattern& pattern, bool& is_pattern_valid, int performan
     set_in_exclusion_optimize_redundancy();
 }
 
+Schedule::Schedule(const Pattern& pattern, const std::vector<int>& order, const PairList& pairs,
+                   bool use_in_exclusion_optimize, int restricts_type, bool& is_pattern_valid) {
+    const int n = pattern.get_size();
+    if (n < 1 || n > 8 || (int)order.size() != n)
+        throw std::invalid_argument("Schedule: order must be a permutation of the pattern's vertices");
+    std::vector<int> seen(n, 0);
+    for (int x : order) {
+        if (x < 0 || x >= n || seen[x]++) throw std::invalid_argument("Schedule: order is not a permutation");
+    }
+    for (const auto& pr : pairs)
+        if (pr.first < 0 || pr.first >= n || pr.second < 0 || pr.second >= n || pr.first >= pr.second)
+            throw std::invalid_argument("Schedule: restriction pairs must satisfy 0 <= first < second < n");
+    size = n;
+    is_pattern_valid = true;
+    adj_mat = reorder(pattern.get_adj_mat_ptr(), n, order);
+    if (use_in_exclusion_optimize) {
+        std::vector<int> identity(n);
+        std::iota(identity.begin(), identity.end(), 0);
+        in_exclusion_optimize_num = get_vec_optimize_num(identity);
+        if (in_exclusion_optimize_num <= 1) in_exclusion_optimize_num = 0;
+        else init_in_exclusion_optimize();
+    } else {
+        in_exclusion_optimize_num = 0;
+    }
+    init_tables();
+    if (!order_is_connected()) {
+        is_pattern_valid = false;
+        return;
+    }
+    build_loop_invariant();
+    if (restricts_type != 0) add_restrict(pairs);
+    set_in_exclusion_optimize_redundancy();
+}
+
+std::vector<Schedule::Candidate> Schedule::candidates(const Pattern& pattern, int perf, int restricts_type, int v_cnt,
+                                                      unsigned int e_cnt, long long tri_cnt) {
+    // the scan of the 8-argument constructor (src/schedule.cpp:30-139)
+    const int n = pattern.get_size();
+    std::vector<Candidate> out;
+    Schedule probe;  // the pattern as given, no tables
+    probe.size = n;
+    probe.adj_mat.assign(pattern.get_adj_mat_ptr(), pattern.get_adj_mat_ptr() + n * n);
+    std::vector<std::vector<int> > cands = all_permutations(n);
+    probe.remove_invalid_permutation(cands);
+    if (perf == 1) {
+        int best_k = 0;
+        for (const auto& c : cands) best_k = std::max(best_k, probe.get_vec_optimize_num(c));
+        std::vector<std::vector<int> > kept;
+        for (const auto& c : cands)
+            if (probe.get_vec_optimize_num(c) == best_k) kept.push_back(c);
+        cands.swap(kept);
+    }
+    auto score = [&](const std::vector<int>& order, const PairList& pairs) {
+        if (perf == 2) return probe.GraphZero_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
+        if (perf == 3) return probe.Naive_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
+        return probe.our_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt, tri_cnt);
+    };
+    for (const auto& order : cands) {
+        std::vector<int> cur = reorder(pattern.get_adj_mat_ptr(), n, order);
+        std::vector<PairList> options;
+        if (restricts_type == 1) {
+            probe.restricts_generate(cur.data(), options);
+        } else {
+            Schedule s(cur.data(), n);
+            PairList pairs;
+            s.GraphZero_aggressive_optimize(pairs);
+            options.push_back(pairs);
+        }
+        if (options.empty()) options.push_back(PairList());
+        for (const auto& pairs : options) out.push_back(Candidate{order, pairs, score(order, pairs)});
+    }
+    return out;
+}
+
 Schedule::Schedule(const int* adj, int n) {
     if (n < 1 || n > 8) throw std::invalid_argument("Schedule: pattern size must be in 1..8");
     size = n;

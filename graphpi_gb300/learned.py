@@ -1,0 +1,215 @@
+"""Learned schedule choice.
+
+GraphPi's Schedule picks a loop order and restriction set by minimising an
+analytic cost (reference src/schedule.cpp:30-139, 1487-1574).  Here a small
+MLP (gpm_mlp_*: hand-written forward/backward/Adam kernels) predicts the
+log runtime of every candidate instead, trained on runtimes the GPU
+enumerator itself measures; the analytic model remains the fallback (no
+model, or a pattern size the model was not trained for) and measured
+runtime the judge.  Every candidate is an exact schedule, so counts do not
+change with the choice.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+
+from . import native
+from .api import Graph, Pattern, Plan, Schedule, schedule_candidates, schedule_from_order
+from .native import U128, check, lib
+
+N_FEATURES = 32
+
+
+def graph_stats(g: Graph) -> dict:
+    return {"v_cnt": g.v_cnt, "e_cnt": g.e_cnt, "tri_cnt": g.ensure_tri_cnt(), "max_degree": g.max_degree}
+
+
+def schedule_features(s: Schedule, stats: dict, analytic_cost: float) -> np.ndarray:
+    """Fixed-length description of a schedule on a graph."""
+    n = s.size
+    adj = s.adj_mat
+    f = np.zeros(N_FEATURES, dtype=np.float32)
+    for d in range(min(n, 8)):
+        f[d] = float(adj[d, :d].sum())  # earlier neighbours of depth d (sets intersected)
+    rcount = [0] * 8
+    for d in range(n):
+        i = s.restrict_last[d]
+        while i != -1:
+            rcount[d] += 1
+            i = s.restrict_next[i]
+    f[8:16] = rcount
+    k = s.in_exclusion_optimize_num
+    f[16] = n
+    f[17] = k
+    f[18] = (n - k) if k else (n - 1)
+    f[19] = s.total_prefix_num
+    f[20] = s.total_restrict_num
+    f[21] = math.log2(max(1, s.in_exclusion_optimize_redundancy))
+    f[22] = math.log2(max(2, stats["v_cnt"]))
+    f[23] = math.log2(max(2, stats["e_cnt"]))
+    f[24] = math.log2(max(2, stats["tri_cnt"] + 1))
+    f[25] = math.log2(max(2, stats["max_degree"]))
+    f[26] = math.log10(max(1e-30, analytic_cost))
+    # restrictions that bind the deepest levels prune the most work
+    f[27] = sum(rcount[max(0, n - 2):n])
+    f[28] = sum(1 for d in range(1, n) if s.father_prefix_id[s.loop_set_prefix_id[d]] == -1)
+    f[29] = float(s.label_sensitive())
+    f[30] = f[26] * f[18]
+    f[31] = 1.0
+    return f
+
+
+def _time_schedule(g: Graph, s: Schedule, max_launch_ms: float = 150.0, cap_ms: float = 3.0e6) -> float:
+    """Estimated full-run kernel time (ms): one interleaved stripe, sized so
+    the launch stays short, scaled up by the stripe count."""
+    plan = Plan(s)
+    gh = g.device()
+    out = U128()
+
+    def run(stripes: int) -> float:
+        native.set_option("raw_sums", 1)
+        native.set_option("stripes", stripes)
+        native.set_option("stripe", stripes // 2)
+        try:
+            check(lib().gpm_count(gh, plan.handle, C.byref(out)), "gpm_count")
+        finally:
+            native.set_option("stripes", 1)
+            native.set_option("stripe", 0)
+            native.set_option("raw_sums", 0)
+        return native.last_launch_stats()[0]
+
+    try:
+        S = 4096
+        t = run(S)
+        est = t * S
+        if est > cap_ms:
+            return est
+        while S > 1 and est / (S // 2) <= max_launch_ms:
+            S //= 2
+        return run(S) * S
+    finally:
+        plan.close()
+
+
+def collect(g: Graph, patterns: list[Pattern], max_candidates: int = 32, use_iep: bool = True,
+            verbose: bool = False) -> list[dict]:
+    """Measures candidate schedules of every pattern on g (GPU)."""
+    stats = graph_stats(g)
+    rows = []
+    for pi, p in enumerate(patterns):
+        cands = schedule_candidates(p, 1, 1, stats["v_cnt"], stats["e_cnt"], stats["tri_cnt"])
+        idx = list(range(len(cands)))
+        if len(idx) > max_candidates:
+            step = len(idx) / max_candidates
+            idx = sorted({int(i * step) for i in range(max_candidates)})
+            # always include the analytic choice
+            best = min(range(len(cands)), key=lambda i: (cands[i]["cost"], i))
+            if best not in idx:
+                idx[-1] = best
+        for i in idx:
+            c = cands[i]
+            s = schedule_from_order(p, c["order"], c["pairs"], use_iep, 1)
+            ms = _time_schedule(g, s)
+            rows.append({"pattern": pi, "cand": i, "features": schedule_features(s, stats, c["cost"]),
+                         "ms": ms, "cost": c["cost"], "order": c["order"], "pairs": c["pairs"]})
+        if verbose:
+            print(f"[learned] pattern {pi}: {len(idx)} candidates", flush=True)
+    return rows
+
+
+class CostModel:
+    """MLP over standardised features predicting log10(ms)."""
+
+    def __init__(self, hidden: int = 64, seed: int = 1):
+        self.hidden = hidden
+        h = C.c_void_p()
+        check(lib().gpm_mlp_create(N_FEATURES, hidden, seed, C.byref(h)), "gpm_mlp_create")
+        self.h = h
+        self.mu = np.zeros(N_FEATURES, dtype=np.float32)
+        self.sd = np.ones(N_FEATURES, dtype=np.float32)
+
+    @property
+    def n_params(self) -> int:
+        return self.hidden * N_FEATURES + 2 * self.hidden + 1
+
+    def _x(self, feats: np.ndarray) -> np.ndarray:
+        return np.ascontiguousarray(((feats - self.mu) / self.sd).astype(np.float32))
+
+    def fit(self, rows: list[dict], epochs: int = 3000, lr: float = 3e-3, weight_decay: float = 1e-4) -> float:
+        X = np.stack([r["features"] for r in rows]).astype(np.float32)
+        y = np.array([math.log10(max(r["ms"], 1e-3)) for r in rows], dtype=np.float32)
+        self.mu = X.mean(axis=0)
+        self.sd = X.std(axis=0) + 1e-3
+        Xs = self._x(X)
+        loss = C.c_float()
+        check(lib().gpm_mlp_train(self.h, Xs.ctypes.data, y.ctypes.data, len(y), epochs, lr, weight_decay,
+                                  C.byref(loss)), "gpm_mlp_train")
+        return loss.value
+
+    def predict(self, feats: np.ndarray) -> np.ndarray:
+        Xs = self._x(np.atleast_2d(feats))
+        y = np.zeros(len(Xs), dtype=np.float32)
+        check(lib().gpm_mlp_forward(self.h, Xs.ctypes.data, len(Xs), y.ctypes.data), "gpm_mlp_forward")
+        return y
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, dtype=np.float32)
+        check(lib().gpm_mlp_params(self.h, p.ctypes.data, len(p), 0), "gpm_mlp_params")
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(lib().gpm_mlp_params(self.h, p.ctypes.data, len(p), 1), "gpm_mlp_params")
+
+    def close(self) -> None:
+        if self.h:
+            lib().gpm_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = True) -> tuple[Schedule, dict]:
+    """Learned schedule choice (analytic model when model is None)."""
+    stats = graph_stats(g)
+    cands = schedule_candidates(pattern, 1, 1, stats["v_cnt"], stats["e_cnt"], stats["tri_cnt"])
+    if model is None:
+        i = min(range(len(cands)), key=lambda j: (cands[j]["cost"], j))
+        c = cands[i]
+        return schedule_from_order(pattern, c["order"], c["pairs"], use_iep, 1), {"index": i, "by": "analytic"}
+    scheds = [schedule_from_order(pattern, c["order"], c["pairs"], use_iep, 1) for c in cands]
+    feats = np.stack([schedule_features(s, stats, c["cost"]) for s, c in zip(scheds, cands)])
+    pred = model.predict(feats)
+    i = int(np.argmin(pred))
+    return scheds[i], {"index": i, "by": "mlp", "pred_log10_ms": float(pred[i])}
+
+
+def evaluate(rows: list[dict], model: CostModel) -> dict:
+    """Per pattern: measured time of the MLP's pick, the analytic pick and
+    the best candidate (from measured rows)."""
+    by_pat: dict[int, list[dict]] = {}
+    for r in rows:
+        by_pat.setdefault(r["pattern"], []).append(r)
+    tot = {"mlp": 0.0, "analytic": 0.0, "best": 0.0}
+    per = []
+    for pi, rs in sorted(by_pat.items()):
+        pred = model.predict(np.stack([r["features"] for r in rs]))
+        m = rs[int(np.argmin(pred))]["ms"]
+        a = min(rs, key=lambda r: (r["cost"], r["cand"]))["ms"]
+        b = min(r["ms"] for r in rs)
+        tot["mlp"] += m
+        tot["analytic"] += a
+        tot["best"] += b
+        per.append({"pattern": pi, "mlp_ms": m, "analytic_ms": a, "best_ms": b})
+    tot["mlp_over_best"] = tot["mlp"] / max(tot["best"], 1e-9)
+    tot["analytic_over_best"] = tot["analytic"] / max(tot["best"], 1e-9)
+    tot["per_pattern"] = per
+    return tot

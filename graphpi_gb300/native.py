@@ -51,6 +51,8 @@ SIGNATURES = {
     "gpm_pattern_multiplicity": (I32, [I32, P, PI64]),
     "gpm_schedule_build": (I32, [I32, P, I32, I32, I32, I64, U64, I64, P, I32, PI32, PI32]),
     "gpm_schedule_analyze": (I32, [P, I32, PI32]),
+    "gpm_schedule_candidates": (I32, [I32, P, I32, I32, I64, U64, I64, P, P, P, P, I32, PI32]),
+    "gpm_schedule_from_order": (I32, [I32, P, P, I32, P, I32, I32, P, I32, PI32, PI32]),
     "gpm_plan_create": (I32, [P, I32, C.POINTER(P)]),
     "gpm_plan_destroy": (I32, [P]),
     "gpm_count": (I32, [P, P, C.POINTER(U128)]),
@@ -66,6 +68,12 @@ SIGNATURES = {
     "gpm_csr_from_edges": (I32, [I32, I64, P, P, C.POINTER(PU32), C.POINTER(PI32)]),
     "gpm_csr_relabel_degree": (I32, [I32, P, P, C.POINTER(PU32), C.POINTER(PI32)]),
     "gpm_free": (None, [P]),
+    "gpm_mlp_create": (I32, [I32, I32, U64, C.POINTER(P)]),
+    "gpm_mlp_destroy": (I32, [P]),
+    "gpm_mlp_params": (I32, [P, P, I32, I32]),
+    "gpm_mlp_forward": (I32, [P, P, I32, P]),
+    "gpm_mlp_gradients": (I32, [P, P, P, I32, P, C.POINTER(C.c_float)]),
+    "gpm_mlp_train": (I32, [P, P, P, I32, I32, C.c_float, C.c_float, C.POINTER(C.c_float)]),
 }
 
 _lib = None

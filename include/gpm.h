@@ -124,6 +124,28 @@ GPM_API int gpm_schedule_build(int32_t n, const int32_t* adj, int32_t perf_type,
                                uint64_t e_cnt, int64_t tri_cnt, int64_t* tables, int32_t cap,
                                int32_t* n_words, int32_t* valid);
 
+/* The candidates the Schedule constructor scores (src/schedule.cpp:30-139):
+ * every valid loop order (for perf_type 1 only those with the longest
+ * inclusion–exclusion tail) times every verified restriction set, in the
+ * constructor's scan order.  For candidate i: orders[i*n .. i*n+n) (new
+ * vertex j = pattern vertex orders[i*n+j]), n_pairs[i] restriction pairs in
+ * pairs[i*2*GPM_MAX_PAIRS ..], and costs[i], the cost the chosen model
+ * assigns (lower is preferred).  *count receives the total; at most cap are
+ * written. */
+#define GPM_MAX_PAIRS 28
+GPM_API int gpm_schedule_candidates(int32_t n, const int32_t* adj, int32_t perf_type, int32_t restricts_type,
+                                    int64_t v_cnt, uint64_t e_cnt, int64_t tri_cnt, int32_t* orders,
+                                    int32_t* n_pairs, int32_t* pairs, double* costs, int32_t cap,
+                                    int32_t* count);
+
+/* The tables (layout of gpm_schedule_build) of the schedule for one
+ * candidate: the pattern relabelled by `order`, restrictions `pairs` (dropped
+ * when restricts_type is 0), inclusion–exclusion as requested — what the
+ * Schedule constructor builds when its model picks that candidate. */
+GPM_API int gpm_schedule_from_order(int32_t n, const int32_t* adj, const int32_t* order, int32_t n_pairs,
+                                    const int32_t* pairs, int32_t use_iep, int32_t restricts_type,
+                                    int64_t* tables, int32_t cap, int32_t* n_words, int32_t* valid);
+
 /* Host-side analysis of schedule tables: *label_sensitive = 1 when the
  * schedule's count depends on the vertex labelling.  The reference's
  * inclusion–exclusion tail skips the restrictions of its own loops and
@@ -175,6 +197,31 @@ GPM_API int gpm_batch_exec_destroy(gpm_batch_exec* exec);
 GPM_API int gpm_count_host(int32_t v_cnt, const uint32_t* rowptr, const int32_t* col,
                            int32_t n_plans, const int64_t* tables, const int32_t* n_words,
                            gpm_u128* outs);
+
+/* ------------------------------------------------------------------ */
+/* learned schedule cost model                                         */
+/* ------------------------------------------------------------------ */
+
+/* A two-layer perceptron (in_dim -> hidden ReLU -> 1, fp32) that predicts
+ * the log runtime of a candidate schedule from its features; the learned
+ * replacement for the scoring in Schedule::our_estimate_schedule_restrict
+ * (src/schedule.cpp:1487-1574), whose analytic model stays the fallback.
+ * Forward, backward and Adam are hand-written kernels on the current device.
+ * Parameters are one flat float array: W1[hidden][in_dim], b1[hidden],
+ * W2[hidden], b2 (hidden*in_dim + 2*hidden + 1 floats). */
+typedef struct gpm_mlp gpm_mlp;
+GPM_API int gpm_mlp_create(int32_t in_dim, int32_t hidden, uint64_t seed, gpm_mlp** out);
+GPM_API int gpm_mlp_destroy(gpm_mlp* m);
+/* copies the parameters out (set = 0) or in (set = 1; resets Adam state) */
+GPM_API int gpm_mlp_params(gpm_mlp* m, float* params, int32_t n_params, int32_t set);
+/* Y[i] = model(X[i*in_dim ..]) for n_rows rows (host arrays) */
+GPM_API int gpm_mlp_forward(gpm_mlp* m, const float* X, int32_t n_rows, float* Y);
+/* gradient of the mean squared error against targets T, and the loss */
+GPM_API int gpm_mlp_gradients(gpm_mlp* m, const float* X, const float* T, int32_t n_rows, float* grads,
+                              float* loss);
+/* full-batch Adam for `epochs` steps; *final_loss = loss before the last step */
+GPM_API int gpm_mlp_train(gpm_mlp* m, const float* X, const float* T, int32_t n_rows, int32_t epochs, float lr,
+                          float weight_decay, float* final_loss);
 
 /* ------------------------------------------------------------------ */
 /* tuning                                                              */

@@ -18,7 +18,23 @@ public:
              int restricts_type, bool use_in_exclusion_optimize, int v_cnt, unsigned int e_cnt,
              long long tri_cnt = 0);
     Schedule(const int* adj_mat, int size);
+    // The schedule the constructor above would build had its cost model
+    // picked `order` (new vertex i = pattern vertex order[i]) and restriction
+    // set `pairs` (in the reordered numbering).  restricts_type 0 drops the
+    // pairs, as the constructor does.
+    Schedule(const Pattern& pattern, const std::vector<int>& order, const std::vector<std::pair<int, int> >& pairs,
+             bool use_in_exclusion_optimize, int restricts_type, bool& is_pattern_valid);
     ~Schedule();
+
+    // Every (loop order, restriction set) the constructor scores for these
+    // inputs, in its scan order, with the cost its model assigns.
+    struct Candidate {
+        std::vector<int> order;
+        std::vector<std::pair<int, int> > pairs;
+        double cost;
+    };
+    static std::vector<Candidate> candidates(const Pattern& pattern, int performance_modeling_type, int restricts_type,
+                                             int v_cnt, unsigned int e_cnt, long long tri_cnt);
 
     inline int get_total_prefix_num() const { return total_prefix_num; }
     inline int get_father_prefix_id(int prefix_id) const { return father_prefix_id[prefix_id]; }
@@ -68,6 +84,7 @@ public:
     std::vector<std::pair<int, int> > restrict_pair;
 
 private:
+    Schedule() = default;  // for the candidate scan
     int size = 0;
     std::vector<int> adj_mat;
     std::vector<int> father_prefix_id, last, next, loop_set_prefix_id;

@@ -1,0 +1,97 @@
+"""Learned schedule cost model: the MLP kernels against a numpy restatement
+(forward, mean-squared-error gradients), training, and the learned choice
+of loop order (exact counts, runtime against the analytic model)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import graphpi_gb300 as gp
+from graphpi_gb300 import learned
+from graphpi_gb300.native import check, lib
+
+
+def np_forward(p, X, H):
+    D = X.shape[1]
+    W1 = p[:H * D].reshape(H, D)
+    b1 = p[H * D:H * D + H]
+    W2 = p[H * D + H:H * D + 2 * H]
+    b2 = p[-1]
+    A = X @ W1.T + b1
+    Hh = np.maximum(A, 0)
+    return Hh @ W2 + b2, Hh, A
+
+
+def np_grads(p, X, T, H):
+    N, D = X.shape
+    Y, Hh, A = np_forward(p, X, H)
+    W2 = p[H * D + H:H * D + 2 * H]
+    dy = 2 * (Y - T) / N
+    gW2 = Hh.T @ dy
+    gb2 = dy.sum()
+    dH = np.outer(dy, W2) * (A > 0)
+    gW1 = dH.T @ X
+    gb1 = dH.sum(axis=0)
+    return np.concatenate([gW1.reshape(-1), gb1, gW2, [gb2]]), np.mean((Y - T) ** 2)
+
+
+def test_feature_vector_shape(engine):
+    s = gp.Schedule(gp.Pattern(gp.PatternType.House), 1, 1, True, 1000, 8000, 500)
+    f = learned.schedule_features(s, {"v_cnt": 1000, "e_cnt": 8000, "tri_cnt": 500, "max_degree": 40}, 1e6)
+    assert f.shape == (learned.N_FEATURES,) and np.all(np.isfinite(f))
+
+
+@pytest.mark.gpu
+def test_mlp_forward_and_gradients_match_cpu(engine):
+    rng = np.random.default_rng(0)
+    m = learned.CostModel(hidden=64, seed=3)
+    p = m.params().astype(np.float64)
+    X = rng.normal(size=(300, learned.N_FEATURES)).astype(np.float32)
+    T = rng.normal(size=300).astype(np.float32)
+    y = np.zeros(300, dtype=np.float32)
+    check(lib().gpm_mlp_forward(m.h, X.ctypes.data, 300, y.ctypes.data), "forward")
+    want, _, _ = np_forward(p, X.astype(np.float64), 64)
+    np.testing.assert_allclose(y, want, rtol=1e-4, atol=1e-4)
+    g = np.zeros(m.n_params, dtype=np.float32)
+    loss = C.c_float()
+    check(lib().gpm_mlp_gradients(m.h, X.ctypes.data, T.ctypes.data, 300, g.ctypes.data, C.byref(loss)), "grad")
+    gw, lw = np_grads(p, X.astype(np.float64), T.astype(np.float64), 64)
+    np.testing.assert_allclose(g, gw, rtol=1e-3, atol=1e-5)
+    assert abs(loss.value - lw) <= 1e-4 * max(1.0, lw)
+    m.close()
+
+
+@pytest.mark.gpu
+def test_mlp_training_fits_a_smooth_target(engine):
+    rng = np.random.default_rng(1)
+    X = rng.normal(size=(800, learned.N_FEATURES)).astype(np.float32)
+    T = (np.sin(X[:, 0]) + 0.5 * X[:, 1] * X[:, 2] + 0.1 * X[:, 3]).astype(np.float32)
+    m = learned.CostModel(hidden=64, seed=5)
+    loss0 = C.c_float()
+    g = np.zeros(m.n_params, dtype=np.float32)
+    check(lib().gpm_mlp_gradients(m.h, X.ctypes.data, T.ctypes.data, 800, g.ctypes.data, C.byref(loss0)), "grad")
+    fl = C.c_float()
+    check(lib().gpm_mlp_train(m.h, X.ctypes.data, T.ctypes.data, 800, 1500, 3e-3, 0.0, C.byref(fl)), "train")
+    assert fl.value < 0.2 * loss0.value
+    m.close()
+
+
+@pytest.mark.gpu
+def test_learned_choice_exact_and_reported(engine, oracle):
+    g = gp.rmat(12, 8, 0.57, 0.19, 0.19, 6)
+    pats = gp.MotifGenerator(5).generate()
+    train, held = pats[::2], pats[1::2]
+    rows = learned.collect(g, train, max_candidates=12)
+    model = learned.CostModel(hidden=64, seed=2)
+    model.fit(rows, epochs=2000)
+    test_rows = learned.collect(g, held, max_candidates=12)
+    ev = learned.evaluate(test_rows, model)
+    print(f"learned vs best {ev['mlp_over_best']:.3f}, analytic vs best {ev['analytic_over_best']:.3f}")
+    assert ev["mlp_over_best"] >= 1.0 and ev["analytic_over_best"] >= 1.0
+    # whatever is chosen counts exactly
+    tri = g.triangle_counting_mt()
+    for p in held[:4]:
+        s_mlp, _ = learned.choose(p, g, model)
+        s_ref = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri)
+        assert g.pattern_matching(s_mlp) == g.pattern_matching(s_ref) == oracle.count(g, s_ref)
+    model.close()

@@ -101,3 +101,16 @@ def test_label_sensitive_schedules_flagged(engine):
     # without inclusion-exclusion nothing is skipped
     for p in gp.motifs_3_to_5():
         assert not gp.Schedule(p, 1, 1, False, 400, 3000, 2000).label_sensitive()
+
+
+def test_candidates_reproduce_the_constructors_choice(engine):
+    # the first candidate of minimal analytic cost, rebuilt from its order,
+    # gives exactly the tables of the Schedule constructor
+    stats = (7115, 201524, 608389)
+    for p in gp.motifs_3_to_5()[::2] + [gp.Pattern(gp.PatternType.House)]:
+        cands = gp.schedule_candidates(p, 1, 1, *stats)
+        assert cands
+        best = min(range(len(cands)), key=lambda i: (cands[i]["cost"], i))
+        s = gp.schedule_from_order(p, cands[best]["order"], cands[best]["pairs"], True, 1)
+        ref = gp.Schedule(p, 1, 1, True, *stats)
+        assert s.tables.tolist() == ref.tables.tolist(), p
