@@ -43,6 +43,26 @@ namespace gpm {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// Internal-check record: the first kernel that detects an impossible state
+// (a merge window that does not advance, an id outside the graph) writes a
+// code and a few values here and skips the work; the host reports it.
+// [0] code, [1..7] values.
+constexpr int kErrMergeStall = 1, kErrBadVertex = 2;
+__device__ unsigned long long g_check[8];
+
+__device__ __noinline__ void record_check(int code, long long a, long long b, long long c, long long d, long long e,
+                                          long long f) {
+    if (atomicCAS(&g_check[0], 0ull, (unsigned long long)code) == 0ull) {
+        g_check[1] = (unsigned long long)a;
+        g_check[2] = (unsigned long long)b;
+        g_check[3] = (unsigned long long)c;
+        g_check[4] = (unsigned long long)d;
+        g_check[5] = (unsigned long long)e;
+        g_check[6] = (unsigned long long)f;
+        __threadfence();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // device building blocks
 
@@ -80,7 +100,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 }
 
 // first index i in a[0, n) with a[i] >= x (all lanes search the same key)
-__device__ __forceinline__ int lower_bound_u(const int* __restrict__ a, int n, int x) {
+__device__ __forceinline__ int lower_bound_u(const int* a, int n, int x) {
     int lo = 0, hi = n;
     while (lo < hi) {
         int mid = (lo + hi) >> 1;
@@ -97,8 +117,8 @@ __device__ __forceinline__ int lower_bound_u(const int* __restrict__ a, int n, i
 // one list.  Found elements are compacted in order (kStore) or counted minus
 // the chosen vertices.
 template <bool kStore>
-__device__ int warp_merge(const int* __restrict__ A, int na, const int* __restrict__ B, int nb,
-                          int* __restrict__ out, const int* chosen, int nch, int lane) {
+__device__ int warp_merge(const int* A, int na, const int* B, int nb, int* out, const int* chosen, int nch,
+                          int lane) {
     int i = 0, j = 0, acc = 0;
     while (i < na && j < nb) {
         const int a = (i + lane < na) ? A[i + lane] : INT_MAX;
@@ -117,8 +137,16 @@ __device__ int warp_merge(const int* __restrict__ A, int na, const int* __restri
         if (kStore && found) out[acc + __popc(fm & lanemask_lt())] = a;
         acc += __popc(fm);
         const int amax = __shfl_sync(kFull, a, 31), bmax = __shfl_sync(kFull, b, 31);
-        i += __popc(__ballot_sync(kFull, a <= bmax));
-        j += __popc(__ballot_sync(kFull, b <= amax));
+        const int di = __popc(__ballot_sync(kFull, a <= bmax));
+        const int dj = __popc(__ballot_sync(kFull, b <= amax));
+        if (di == 0 && dj == 0) {
+            // only possible when a window is not sorted: record and stop
+            const int a0 = __shfl_sync(kFull, a, 0);
+            if (lane == 0) record_check(kErrMergeStall, na, nb, i, j, a0, bmax);
+            break;
+        }
+        i += di;
+        j += dj;
     }
     if (kStore) __syncwarp();
     return acc;
@@ -138,8 +166,7 @@ __device__ __forceinline__ bool prefer_merge(int na, int nb) {
 }
 
 // A ∩ B written sorted to out; returns its size.
-__device__ int isect_store(const int* __restrict__ A, int na, const int* __restrict__ B, int nb,
-                           int* __restrict__ out, int lane) {
+__device__ int isect_store(const int* A, int na, const int* B, int nb, int* out, int lane) {
     if (na > nb) {
         const int* t = A; A = B; B = t;
         int u = na; na = nb; nb = u;
@@ -167,8 +194,8 @@ __device__ int isect_store(const int* __restrict__ A, int na, const int* __restr
 }
 
 // |A ∩ B ∩ [0, bound) \ chosen[0, nch)|
-__device__ int isect_count(const int* __restrict__ A, int na, const int* __restrict__ B, int nb, int bound,
-                           const int* chosen, int nch, int lane) {
+__device__ int isect_count(const int* A, int na, const int* B, int nb, int bound, const int* chosen, int nch,
+                           int lane) {
     na = lower_bound_u(A, na, bound);
     nb = lower_bound_u(B, nb, bound);
     if (na > nb) {
@@ -199,7 +226,7 @@ __device__ int isect_count(const int* __restrict__ A, int na, const int* __restr
 
 // |S[0, len) \ chosen[0, nch)|  (VertexSet::unorderd_subtraction_size,
 // src/vertex_set.cpp:196-209)
-__device__ __forceinline__ int count_outside(const int* __restrict__ S, int len, const int* chosen, int nch, int lane) {
+__device__ __forceinline__ int count_outside(const int* S, int len, const int* chosen, int nch, int lane) {
     bool in = false;
     if (lane < nch) {
         const int c = chosen[lane];
@@ -218,7 +245,7 @@ __device__ __forceinline__ void add128(unsigned long long* o, __int128 v) {
 }
 
 // x in sorted a[0, n) (per-lane search)
-__device__ __forceinline__ bool contains(const int* __restrict__ a, int n, int x) {
+__device__ __forceinline__ bool contains(const int* a, int n, int x) {
     const int p = lower_bound_u(a, n, x);
     return p < n && a[p] == x;
 }
@@ -713,6 +740,10 @@ __global__ void __launch_bounds__(256) tc_kernel(GraphView g, unsigned long long
                 cur_hi = g.rowptr[lo + 1];
             }
             const int u = g.col[e];
+            if ((unsigned)u >= (unsigned)g.v_cnt) {
+                if (lane == 0) record_check(kErrBadVertex, e, u, cur_v, g.v_cnt, 0, 0);
+                continue;
+            }
             if (u >= cur_v) continue;
             const unsigned ub = g.rowptr[u], ue = g.rowptr[u + 1];
             acc += (unsigned long long)isect_count(g.col + cur_lo, (int)(cur_hi - cur_lo), g.col + ub, (int)(ue - ub), u,
@@ -863,6 +894,20 @@ struct DevBuf {
     }
 };
 
+// Reports (and clears) an internal-check record left by a kernel.
+static int take_check(const char* where) {
+    unsigned long long rec[8] = {0};
+    GPM_CK(cudaMemcpyFromSymbol(rec, g_check, sizeof rec));
+    if (rec[0] == 0) return GPM_OK;
+    const unsigned long long zero[8] = {0};
+    cudaMemcpyToSymbol(g_check, zero, sizeof zero);
+    set_error("%s: internal check %llu failed (values %lld %lld %lld %lld %lld %lld)", where, rec[0], (long long)rec[1],
+              (long long)rec[2], (long long)rec[3], (long long)rec[4], (long long)rec[5], (long long)rec[6]);
+    return GPM_ERR_CUDA;
+}
+
+static unsigned validate_csr(DeviceCtx* c, const GraphView& v, int* rc);
+
 static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     const int V = g->v_cnt;
     const unsigned E = (unsigned)g->e_cnt;
@@ -920,7 +965,42 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     g->col = (int32_t*)new_col.p;
     new_col.p = nullptr;
     g->relabelled = true;
+    // the relabelled copy must be as well-formed as the input
+    GraphView nv;
+    nv.rowptr = g->rowptr;
+    nv.col = g->col;
+    nv.v_cnt = g->v_cnt;
+    nv.pad_ = 0;
+    nv.e_cnt = g->e_cnt;
+    int rc = GPM_OK;
+    const unsigned flags = validate_csr(c, nv, &rc);
+    if (rc) return rc;
+    if (flags) {
+        set_error("device relabel produced a malformed CSR (check flags 0x%x)", flags);
+        return GPM_ERR_CUDA;
+    }
     return GPM_OK;
+}
+
+static unsigned validate_csr(DeviceCtx* c, const GraphView& v, int* rc) {
+    unsigned* d_flags = nullptr;
+    unsigned flags = 0;
+    *rc = GPM_OK;
+    if (cudaMalloc(&d_flags, sizeof(unsigned)) != cudaSuccess) {
+        set_error("validate: out of device memory");
+        *rc = GPM_ERR_OOM;
+        return 0;
+    }
+    cudaMemsetAsync(d_flags, 0, sizeof(unsigned), c->stream);
+    validate_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(v, d_flags);
+    cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_flags);
+    if (e != cudaSuccess) {
+        set_error("validate: %s", cudaGetErrorString(e));
+        *rc = GPM_ERR_CUDA;
+    }
+    return flags;
 }
 
 static GraphView view_of(const gpm_graph* g, bool caller_ids = false) {
@@ -1046,7 +1126,7 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     t_launches = 1;
     t_bytes = raw[2 * n];
     memcpy(host_raw, raw.data(), sizeof(unsigned long long) * 2 * n);
-    return GPM_OK;
+    return take_check("pattern matching");
 }
 
 static int finish_counts(int n, const gpm_plan* const* plans, const unsigned long long* raw, gpm_u128* outs) {
@@ -1214,6 +1294,8 @@ GPM_API int gpm_tri_count(gpm_graph* g, uint64_t* out) {
     t_ms = ms;
     t_launches = 1;
     t_bytes = 0;
+    int rc = take_check("gpm_tri_count");
+    if (rc) return rc;
     *out = h[1];
     return GPM_OK;
 }
@@ -1398,6 +1480,8 @@ GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph
     t_launches = 1;
     t_bytes = e->h_small[2 * n];
     std::vector<unsigned long long> raw(e->h_small, e->h_small + 2 * n);
+    int rc = take_check("gpm_batch_exec_run");
+    if (rc) return rc;
     return finish_counts(n, e->plans.data(), raw.data(), outs);
 }
 

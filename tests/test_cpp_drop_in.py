@@ -50,7 +50,7 @@ def test_drop_in_counts_match_oracle(engine, oracle, tmp_path):
     _write_edges(h, path)
     for adj, size in [("0111101111011110", 4), ("0111010011100101100001100", 5)]:
         out = subprocess.run([str(exe), "complete8", str(path), str(size), adj], capture_output=True, text=True,
-                             check=True).stdout
+                             check=True, timeout=120).stdout
         got = int(next(l for l in out.splitlines() if l.startswith("ans ")).split()[1])
         tri = int(next(l for l in out.splitlines() if l.startswith("tri ")).split()[1])
         assert tri == oracle.triangles(h)

@@ -233,3 +233,19 @@ def test_leaf_batch_matches_per_candidate_path(engine, oracle):
         assert gp.batch_count([g] * len(scheds), scheds) == batched
     finally:
         gp.set_option("stage_max", old)
+
+
+def test_uneven_multi_graph_batch(engine, oracle):
+    # the 256-pair uneven batch, shrunk: 24 seeded Chung-Lu graphs with
+    # parameters from the same generator (sizes scaled to 300-3000 vertices),
+    # one motif each, all pairs in one persistent launch; per-pair exact
+    from graphpi_gb300 import workloads
+    motifs = gp.motifs_3_to_5()
+    params = workloads.uneven_params(count=24, n_lo=300, n_hi=3000)
+    graphs, scheds = [], []
+    for n, avg, gamma, seed, m in params:
+        g = workloads.uneven_graph(n, min(avg, 24.0), gamma, seed)
+        graphs.append(g)
+        scheds.append(gp.Schedule(motifs[m], 1, 1, True, g.v_cnt, g.e_cnt, oracle.triangles(g)))
+    got = gp.batch_count(graphs, scheds)
+    assert got == [oracle.count(g, s) for g, s in zip(graphs, scheds)]
