@@ -129,7 +129,9 @@ __device__ int warp_merge(const int* A, int na, const int* B, int nb, int* out, 
             const int bv = __shfl_sync(kFull, b, pos + step - 1);
             if (bv < a) pos += step;
         }
-        bool found = (a != INT_MAX) && (__shfl_sync(kFull, b, pos) == a);
+        // every lane must execute the shuffle (no short-circuit around it)
+        const int bp = __shfl_sync(kFull, b, pos);
+        bool found = (a != INT_MAX) && (bp == a);
         if (!kStore && found)
             for (int q = 0; q < nch; ++q)
                 if (chosen[q] == a) found = false;
