@@ -96,6 +96,9 @@ typedef struct {
     int V;
     const sched_t* s;
     int cap;
+    double deadline;   /* omp_get_wtime() limit; 0: none */
+    long long calls;
+    int expired;
     int* buf[MAXP];
     const int* ptr[MAXP];
     int len[MAXP];
@@ -166,6 +169,8 @@ static int bound_at(const ctx_t* c, int depth) {
 
 static void rec(ctx_t* c, int depth) {
     const sched_t* s = c->s;
+    if (c->deadline > 0 && (++c->calls & 1023) == 0 && omp_get_wtime() > c->deadline) c->expired = 1;
+    if (c->expired) return;
     int lsid = s->loop_set[depth];
     const int* S = c->ptr[lsid];
     int size = c->len[lsid];
@@ -244,13 +249,15 @@ static int max_isect(int V, const uint32_t* rp) {
 /* Raw sum over the roots in `roots` (all roots when roots == NULL) before the
  * division by the redundancy; out = {lo, hi} two's complement. */
 static int run(int V, const uint32_t* rp, const int32_t* col, const int64_t* tables, int nw, const int32_t* roots,
-               int64_t nroots, int threads, uint64_t* out) {
+               int64_t nroots, int threads, double seconds, int64_t* done, uint64_t* out) {
     sched_t s;
     if (parse(tables, nw, &s)) return -1;
     int cap = max_isect(V, rp);
     int64_t total = roots ? nroots : V;
     i128 sum = 0;
     int bad = 0;
+    int64_t completed = 0;
+    const double deadline = seconds > 0 ? omp_get_wtime() + seconds : 0;
 #pragma omp parallel num_threads(threads > 0 ? threads : omp_get_max_threads()) reduction(| : bad)
     {
         ctx_t c;
@@ -260,6 +267,8 @@ static int run(int V, const uint32_t* rp, const int32_t* col, const int64_t* tab
         c.V = V;
         c.s = &s;
         c.cap = cap;
+        c.deadline = deadline;
+        int64_t my_done = 0;
         for (int p = 0; p < s.P; ++p) {
             c.buf[p] = (int*)malloc(sizeof(int) * (size_t)cap);
             if (!c.buf[p]) bad = 1;
@@ -270,20 +279,28 @@ static int run(int V, const uint32_t* rp, const int32_t* col, const int64_t* tab
         if (!bad) {
 #pragma omp for schedule(dynamic, 16)
             for (int64_t r = 0; r < total; ++r) {
+                if (c.expired) continue;
                 int v = roots ? roots[r] : (int)r;
+                i128 before = c.ans;
                 for (int p = s.last[0]; p != -1; p = s.next[p]) build(&c, p, v);
                 c.nchosen = 0;
                 c.chosen[c.nchosen++] = v;
                 rec(&c, 1);
+                if (c.expired) c.ans = before; /* drop the unfinished root */
+                else ++my_done;
             }
         }
 #pragma omp critical
-        sum += c.ans;
+        {
+            sum += c.ans;
+            completed += my_done;
+        }
         for (int p = 0; p < s.P; ++p) free(c.buf[p]);
         free(c.tmp);
         free(c.tmp2);
     }
     if (bad) return -2;
+    if (done) *done = completed;
     out[0] = (uint64_t)sum;
     out[1] = (uint64_t)(sum >> 64);
     return 0;
@@ -294,7 +311,7 @@ int oracle_pattern_matching(int V, const uint32_t* rp, const int32_t* col, const
     uint64_t raw[2];
     sched_t s;
     if (parse(tables, nw, &s)) return -1;
-    int rc = run(V, rp, col, tables, nw, NULL, 0, threads, raw);
+    int rc = run(V, rp, col, tables, nw, NULL, 0, threads, 0, NULL, raw);
     if (rc) return rc;
     i128 sum = (i128)(((unsigned __int128)raw[1] << 64) | raw[0]);
     if (sum < 0) return -3;
@@ -306,7 +323,15 @@ int oracle_pattern_matching(int V, const uint32_t* rp, const int32_t* col, const
 
 int oracle_pattern_matching_roots(int V, const uint32_t* rp, const int32_t* col, const int64_t* tables, int nw,
                                   const int32_t* roots, int64_t nroots, int threads, uint64_t* raw) {
-    return run(V, rp, col, tables, nw, roots, nroots, threads, raw);
+    return run(V, rp, col, tables, nw, roots, nroots, threads, 0, NULL, raw);
+}
+
+/* As above, but stops after `seconds` of wall time: roots not finished by
+ * then are left out; *done receives how many roots were counted in full. */
+int oracle_pattern_matching_roots_timed(int V, const uint32_t* rp, const int32_t* col, const int64_t* tables, int nw,
+                                        const int32_t* roots, int64_t nroots, int threads, double seconds,
+                                        int64_t* done, uint64_t* raw) {
+    return run(V, rp, col, tables, nw, roots, nroots, threads, seconds, done, raw);
 }
 
 long long oracle_triangle_count(int V, const uint32_t* rp, const int32_t* col, int threads) {

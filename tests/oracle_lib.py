@@ -21,6 +21,9 @@ class Oracle:
                                                 C.c_void_p]
         lib.oracle_pattern_matching_roots.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                                       C.c_void_p, C.c_int64, C.c_int, C.c_void_p]
+        lib.oracle_pattern_matching_roots_timed.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                                            C.c_void_p, C.c_int64, C.c_int, C.c_double,
+                                                            C.c_void_p, C.c_void_p]
         lib.oracle_brute_force.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
                                            C.c_void_p]
         lib.oracle_triangle_count.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int]
@@ -44,6 +47,19 @@ class Oracle:
         assert rc == 0, f"oracle failed ({rc})"
         v = int(out[0]) | (int(out[1]) << 64)
         return v - (1 << 128) if v >= (1 << 127) else v
+
+    def raw_roots_timed(self, g, schedule, roots, seconds: float, threads: int = 0) -> tuple[int, int]:
+        """(undivided signed sum over the roots finished within `seconds`, how many)."""
+        t = np.ascontiguousarray(schedule.tables, dtype=np.int64)
+        r = np.ascontiguousarray(roots, dtype=np.int32)
+        out = np.zeros(2, dtype=np.uint64)
+        done = np.zeros(1, dtype=np.int64)
+        rc = self.L.oracle_pattern_matching_roots_timed(g.v_cnt, g.vertex.ctypes.data, g.edge.ctypes.data,
+                                                        t.ctypes.data, len(t), r.ctypes.data, len(r), threads,
+                                                        seconds, done.ctypes.data, out.ctypes.data)
+        assert rc == 0, f"oracle failed ({rc})"
+        v = int(out[0]) | (int(out[1]) << 64)
+        return (v - (1 << 128) if v >= (1 << 127) else v), int(done[0])
 
     def brute_force(self, g, pattern, threads: int = 0) -> int:
         a = np.ascontiguousarray(pattern.adj, dtype=np.int32)
