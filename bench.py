@@ -351,7 +351,7 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--stripes", default=os.environ.get("GPM_BENCH_STRIPES", "auto"),
                     help="stripes per full job, or 'auto' to size a step to --step-seconds")
-    ap.add_argument("--step-seconds", type=float, default=8.0)
+    ap.add_argument("--step-seconds", type=float, default=4.0)
     ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark graph)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     args = ap.parse_args()

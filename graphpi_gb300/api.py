@@ -215,6 +215,14 @@ class Schedule:
         check(lib().gpm_schedule_analyze(t.ctypes.data, len(t), C.byref(out)), "gpm_schedule_analyze")
         return bool(out.value)
 
+    def plan_info(self) -> dict:
+        """How the engine evaluates this schedule (gpm_plan_info)."""
+        t = np.ascontiguousarray(self.tables, dtype=np.int64)
+        info = np.zeros(6, dtype=np.int32)
+        check(lib().gpm_plan_info(t.ctypes.data, len(t), info.ctypes.data, 6), "gpm_plan_info")
+        keys = ("T", "L", "k", "leaf_kind", "pair_ok", "label_sensitive")
+        return dict(zip(keys, map(int, info)))
+
     # reference getters (include/schedule.h:23-37)
     def get_size(self): return self.size
     def get_total_prefix_num(self): return self.total_prefix_num

@@ -242,6 +242,12 @@ int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out) {
             if (built_at[st] == p.L) {
                 p.leaf_kind = kLeafCount;
                 p.leaf_fa = father[st];  // -1: the set is N(v) itself
+                const int L1 = p.L - 1, f = father[st];
+                const bool f_is_nbr = f >= 0 && father[f] < 0 && built_at[f] == L1 &&
+                                      p.chain_begin[L1 + 1] - p.chain_begin[L1] == 1;
+                const bool b_fixed = built_at[p.loop_set[p.L]] < L1 && !((p.rmask[p.L] >> L1) & 1u);
+                const bool t_fixed = (p.rmask[p.T] >> L1) == 0;
+                p.pair_ok = (L1 >= 2 && f_is_nbr && b_fixed && t_fixed) ? 1 : 0;
             }
         } else if (k == 2 && ngroups == 2) {
             // groups {a}{b} and {a,b} in either order
@@ -646,6 +652,24 @@ GPM_API int gpm_schedule_analyze(const int64_t* tables, int32_t n_words, int32_t
     return GPM_OK;
 }
 
+GPM_API int gpm_plan_info(const int64_t* tables, int32_t n_words, int32_t* info, int32_t cap) {
+    gpm::clear_error();
+    if (!info || cap < 6) {
+        set_error("gpm_plan_info: need room for 6 values");
+        return GPM_ERR_INVALID_ARG;
+    }
+    gpm::DevPlan p;
+    int rc = gpm::compile_plan(tables, n_words, &p);
+    if (rc) return rc;
+    info[0] = p.T;
+    info[1] = p.L;
+    info[2] = p.k;
+    info[3] = p.leaf_kind;
+    info[4] = p.pair_ok;
+    info[5] = p.label_sensitive;
+    return GPM_OK;
+}
+
 GPM_API int gpm_set_option(const char* key, int64_t value) {
     gpm::clear_error();
     if (!key) return GPM_ERR_INVALID_ARG;
@@ -660,6 +684,7 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "timeout_ms") slot = &o.timeout_ms, lo = 1, hi = 3600 * 1000;
     else if (k == "stage_max") slot = &o.stage_max, lo = 0, hi = 1 << 14;
     else if (k == "leaf_batch") slot = &o.leaf_batch, lo = 0, hi = 1;
+    else if (k == "pair_leaf") slot = &o.pair_leaf, lo = 0, hi = 1;
     else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
     else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;
     else if (k == "stripe") slot = &o.stripe, lo = 0, hi = (1 << 30) - 1;
@@ -691,6 +716,7 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "timeout_ms") *value = o.timeout_ms;
     else if (k == "stage_max") *value = o.stage_max;
     else if (k == "leaf_batch") *value = o.leaf_batch;
+    else if (k == "pair_leaf") *value = o.pair_leaf;
     else if (k == "split") *value = o.split;
     else if (k == "stripes") *value = o.stripes;
     else if (k == "stripe") *value = o.stripe;

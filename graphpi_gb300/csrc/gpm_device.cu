@@ -91,7 +91,67 @@ struct WarpState {
     const int* lp[kMaxN];
     int blockval[kMaxBlocks];
     int leafcnt[3][32];  // per-candidate counters of a leaf batch
+    unsigned epoch;      // tag of the live entries of this warp's pair-sum table
+    int dslot[kMaxN];    // donation record the loop of depth d draws from (-1: none)
+    unsigned dgen[kMaxN];
+    int downer[kMaxN];   // 1: this warp published that record
 };
+
+// Work donation (hub splitting).  A warp whose loop at depth d >= 2 has at
+// least `split` candidates publishes the loop as a record: the pair, d and
+// chosen[0, d).  From then on the owner and any warp that has finished its
+// own queues take slices [next, next + s) of the loop by compare-and-swap on
+// the record's word; a helper rebuilds the prefix sets of chosen[0, d) and
+// adds what it counts to the pair's sum.  Nothing waits on a record: a warp
+// that finds no free slot runs its loop alone, a claim either succeeds or
+// sees the loop exhausted, and only the owner frees a slot, after the last
+// slice has been taken (helpers keep their own copies of what they need).
+constexpr int kDonSlots = 1024;
+constexpr int kErrDonation = 4;
+
+struct Donation {
+    unsigned long long word;  // generation (16 bits) | end (24) | next (24)
+    int pair;
+    int depth;
+    int chosen[kMaxN];
+    int pad_[4];
+};
+static_assert(sizeof(Donation) == 64, "one record per 64 bytes");
+
+struct DonationArea {
+    Donation rec[kDonSlots];
+    unsigned busy[kDonSlots];  // 1 while a record's owner holds the slot
+    unsigned finished;         // warps done with their own queues
+    unsigned pad_[3];
+};
+
+__device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned end, unsigned next) {
+    return ((unsigned long long)(gen & 0xffffu) << 48) | ((unsigned long long)(end & 0xffffffu) << 24) |
+           (unsigned long long)(next & 0xffffffu);
+}
+
+// Takes the next slice of record r (generation gen); lo == hi when the loop
+// is exhausted or the slot holds another generation.  Lock-free: a failed
+// compare-and-swap means another warp took a slice, so the retries are
+// bounded by the loop length (< 2^24).
+__device__ void don_claim(Donation* r, unsigned gen, int& lo, int& hi) {
+    lo = hi = 0;
+    unsigned long long w = *(volatile unsigned long long*)&r->word;
+    for (int tries = 0; tries < (1 << 25); ++tries) {
+        if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
+        const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
+        if (next >= end) return;
+        const unsigned take = min(64u, max(1u, (end - next) >> 5));
+        const unsigned long long got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
+        if (got == w) {
+            lo = (int)next;
+            hi = (int)(next + take);
+            return;
+        }
+        w = got;
+    }
+    record_check(kErrDonation, gen, (long long)w, 0, 0, 0, 0);
+}
 
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
@@ -246,6 +306,51 @@ __device__ __forceinline__ void add128(unsigned long long* o, __int128 v) {
     if (hi + carry) atomicAdd(o + 1, hi + carry);
 }
 
+// Pair-sum table entries: epoch (16 bits) | vertex (24 bits) | count (24 bits).
+// A slot whose epoch differs from the warp's current one is empty.
+__device__ __forceinline__ unsigned long long pair_word(unsigned epoch, int x, unsigned cnt) {
+    return ((unsigned long long)(epoch & 0xffffu) << 48) | ((unsigned long long)(x & 0xffffff) << 24) | cnt;
+}
+
+__device__ __forceinline__ unsigned pair_slot(int x, unsigned mask) { return ((unsigned)x * 2654435761u) >> 7 & mask; }
+
+// adds one to x's count; false when the table is full (never at load <= 1/2)
+__device__ bool pair_add(unsigned long long* T, unsigned mask, unsigned epoch, int x) {
+    unsigned slot = pair_slot(x, mask);
+    for (unsigned probes = 0; probes <= mask; ++probes) {
+        unsigned long long old = T[slot];
+        for (;;) {
+            const bool live = (unsigned)(old >> 48) == (epoch & 0xffffu);
+            if (live && (int)((old >> 24) & 0xffffff) == x) {
+                const unsigned long long got = atomicCAS(&T[slot], old, old + 1);
+                if (got == old) return true;
+                old = got;
+                continue;
+            }
+            if (!live) {
+                const unsigned long long got = atomicCAS(&T[slot], old, pair_word(epoch, x, 1));
+                if (got == old) return true;
+                old = got;
+                continue;
+            }
+            break;  // live entry of another vertex: next slot
+        }
+        slot = (slot + 1) & mask;
+    }
+    return false;
+}
+
+__device__ unsigned pair_get(const unsigned long long* T, unsigned mask, unsigned epoch, int x) {
+    unsigned slot = pair_slot(x, mask);
+    for (unsigned probes = 0; probes <= mask; ++probes) {
+        const unsigned long long w = T[slot];
+        if ((unsigned)(w >> 48) != (epoch & 0xffffu)) return 0;
+        if ((int)((w >> 24) & 0xffffff) == x) return (unsigned)(w & 0xffffff);
+        slot = (slot + 1) & mask;
+    }
+    return 0;
+}
+
 // x in sorted a[0, n) (per-lane search)
 __device__ __forceinline__ bool contains(const int* a, int n, int x) {
     const int p = lower_bound_u(a, n, x);
@@ -263,6 +368,13 @@ struct WarpCtx {
     int leaf_on;
     int* stage;      // 2 * stage_cap ints of this warp's shared memory
     int stage_cap;
+    int pair_on;
+    unsigned long long* ptab;  // this warp's pair-sum table (pmask + 1 words)
+    unsigned pmask;
+    DonationArea* don;         // null: no donation
+    int split_min;             // smallest loop that is donated
+    int pair_idx;              // pair whose work is running
+    long long gw;              // global warp index
     unsigned long long bytes;
 
     // copies a fixed set into shared-memory region r when it fits
@@ -302,6 +414,105 @@ struct WarpCtx {
         bool hit = false;
         for (int q = 0; q < L; ++q) hit |= s->chosen[q] == x;
         return hit;
+    }
+
+    // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
+    // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
+    // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
+    // (and does nothing) when B's neighbour lists would fill the table more
+    // than half: the caller then runs the level normally.
+    __device__ bool pair_level(__int128& out) {
+        const int L1 = P->L - 1;
+        const int T = P->T;
+        const int* candA = s->lp[L1];
+        const int na = s->end[L1];
+        const int sb = P->loop_set[P->L];
+        const int* candB = s->ptr[sb];
+        const int nb = lower_bound_u(candB, s->len[sb], bound_of(P->L));
+        const int bnd = bound_of(T);
+        // size of B's neighbour lists below the bound
+        long long mb = 0;
+        for (int base = 0; base < nb; base += 32) {
+            const int j = base + lane;
+            int len = 0;
+            if (j < nb) {
+                const int w = candB[j];
+                if (!chosen_before(w, L1)) {
+                    const unsigned st = g.rowptr[w];
+                    len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
+                }
+            }
+            int pre;
+            mb += warp_scan(len, pre);
+        }
+        if (mb * 2 > (long long)pmask + 1) return false;
+        if (lane == 0) {
+            s->epoch = (s->epoch + 1) & 0xffffu;
+            if (s->epoch == 0) s->epoch = 1;
+        }
+        __syncwarp();
+        const unsigned ep = s->epoch;
+        if (ep == 1) {  // fresh cycle of tags: clear the table
+            for (unsigned i = lane; i <= pmask; i += 32) ptab[i] = 0ull;
+            __syncwarp();
+        }
+        long long sum = 0;
+        // phase 1 (B -> counts) and phase 2 (A -> sum of counts)
+        for (int phase = 0; phase < 2; ++phase) {
+            const int* cand = phase == 0 ? candB : candA;
+            const int nc = phase == 0 ? nb : na;
+            for (int base = 0; base < nc; base += 32) {
+                const int j = base + lane;
+                unsigned st = 0;
+                int len = 0;
+                if (j < nc) {
+                    const int v = cand[j];
+                    if (!chosen_before(v, L1)) {
+                        st = g.rowptr[v];
+                        len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
+                        if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
+                    }
+                }
+                int pre;
+                const int M = warp_scan(len, pre);
+                for (int eb = 0; eb < M; eb += 32) {
+                    const int e = eb + lane;
+                    const int c = owner(pre, e);
+                    const unsigned stc = __shfl_sync(kFull, st, c);
+                    const int prc = __shfl_sync(kFull, pre, c);
+                    if (e < M) {
+                        const int x = g.col[stc + (e - prc)];
+                        if (!chosen_before(x, L1)) {
+                            if (phase == 0) {
+                                if (!pair_add(ptab, pmask, ep, x)) record_check(3, x, mb, pmask, 0, 0, 0);
+                            } else {
+                                sum += pair_get(ptab, pmask, ep, x);
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // c term: v in both candidate lists pairs with itself
+        for (int base = 0; base < na; base += 32) {
+            const int j = base + lane;
+            if (j < na) {
+                const int v = candA[j];
+                if (!chosen_before(v, L1) && contains(candB, nb, v)) {
+                    const unsigned st = g.rowptr[v];
+                    const int* nv = g.col + st;
+                    const int len = lower_bound_u(nv, (int)(g.rowptr[v + 1] - st), bnd);
+                    int in = 0;
+                    for (int q = 0; q < L1; ++q) in += contains(nv, len, s->chosen[q]) ? 1 : 0;
+                    sum -= (long long)(len - in);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+        out = lane == 0 ? (__int128)sum : (__int128)0;
+        return true;
     }
 
     // All candidates of level L at once (the plan's leaf_kind says how the
@@ -577,21 +788,89 @@ struct WarpCtx {
             s->lp[d] = S;
             s->idx[d] = 0;
             s->end[d] = e;
+            s->dslot[d] = -1;
         }
         __syncwarp();
     }
 
-    // levels 2..L below a fixed (v0, v1)
-    __device__ __int128 dfs_from_2() {
+    // Publishes the loop of depth d (just started) when it is long enough
+    // and a slot is free; the owner's own range then comes from claims.
+    __device__ void maybe_donate(int d) {
+        if (!don || split_min <= 0) return;
+        const int e = s->end[d];
+        if (e < split_min || e > 0xffffff) return;
+        if (lane == 0) {
+            int h = -1;
+            for (int probe = 0; probe < 4 && h < 0; ++probe) {
+                const int c = (int)((gw * 7 + d * 131 + probe * 257) & (kDonSlots - 1));
+                if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
+            }
+            if (h >= 0) {
+                Donation* r = &don->rec[h];
+                volatile Donation* vr = r;
+                const unsigned gen = ((unsigned)(vr->word >> 48) + 1u) & 0xffffu;
+                vr->pair = pair_idx;
+                vr->depth = d;
+                for (int j = 0; j < d; ++j) vr->chosen[j] = s->chosen[j];
+                __threadfence();
+                atomicExch(&r->word, don_pack(gen, (unsigned)e, 0u));
+                s->dslot[d] = h;
+                s->dgen[d] = gen;
+                s->downer[d] = 1;
+                s->end[d] = 0;
+            }
+        }
+        __syncwarp();
+    }
+
+    // next slice of the donated loop at depth d into idx[d], end[d]
+    __device__ bool claim_more(int d) {
+        int lo = 0, hi = 0;
+        if (lane == 0) {
+            don_claim(&don->rec[s->dslot[d]], s->dgen[d], lo, hi);
+            if (hi > lo) {
+                s->idx[d] = lo;
+                s->end[d] = hi;
+            }
+        }
+        hi = __shfl_sync(kFull, hi, 0);
+        lo = __shfl_sync(kFull, lo, 0);
+        __syncwarp();
+        return hi > lo;
+    }
+
+    // the donated loop at depth d is exhausted: its owner frees the slot
+    __device__ void release(int d) {
+        if (lane == 0) {
+            if (s->downer[d]) {
+                __threadfence();
+                atomicExch(&don->busy[s->dslot[d]], 0u);
+            }
+            s->dslot[d] = -1;
+        }
+        __syncwarp();
+    }
+
+    __device__ __forceinline__ bool batch_on() const { return leaf_on && P->leaf_kind != kLeafGeneric; }
+    // pair-sum table keys are 24-bit ids
+    __device__ __forceinline__ bool pair_ready() const { return pair_on && P->pair_ok && g.v_cnt <= (1 << 24); }
+
+    // Loops of depths d0..L; chosen[0, d0), their prefix sets and the loop
+    // range of depth d0 are set.  Returns when depth d0's range (and, for a
+    // donated loop, every slice of it) is done.
+    __device__ __int128 dfs_levels(int d0) {
         const int L = P->L;
-        const bool batch = leaf_on && P->leaf_kind != kLeafGeneric;
+        const bool batch = batch_on();
+        const bool pair = pair_ready();
         __int128 acc = 0;
-        int d = 2;
-        start_level(2);
-        if (batch && L == 2) return leaf_batch();
-        while (d >= 2) {
+        int d = d0;
+        while (d >= d0) {
             const int i = s->idx[d];
             if (i >= s->end[d]) {
+                if (s->dslot[d] >= 0) {
+                    if (claim_more(d)) continue;
+                    release(d);
+                }
                 --d;
                 continue;
             }
@@ -615,9 +894,128 @@ struct WarpCtx {
             if (batch && d == L) {
                 acc += leaf_batch();
                 --d;
+                continue;
             }
+            if (pair && d == L - 1) {
+                __int128 r;
+                if (pair_level(r)) {
+                    acc += r;
+                    --d;
+                    continue;
+                }
+            }
+            maybe_donate(d);
         }
         return acc;
+    }
+
+    // levels 2..L below a fixed (v0, v1)
+    __device__ __int128 dfs_from_2() {
+        const int L = P->L;
+        start_level(2);
+        if (batch_on() && L == 2) return leaf_batch();
+        if (pair_ready() && L == 3) {
+            __int128 r;
+            if (pair_level(r)) return r;
+        }
+        maybe_donate(2);
+        return dfs_levels(2);
+    }
+
+    // Takes slices of record h (generation gen) until it is exhausted;
+    // false when nothing could be taken.
+    __device__ bool help_one(const PairDesc* pairs, int npairs, unsigned long long* out, int h, unsigned gen) {
+        Donation* r = &don->rec[h];
+        int lo = 0, hi = 0, p = 0, d = 0, rend = 0;
+        if (lane == 0) {
+            const unsigned long long w = *(volatile unsigned long long*)&r->word;
+            if ((unsigned)(w >> 48) == gen && (w & 0xffffffu) < ((w >> 24) & 0xffffffu)) {
+                __threadfence();
+                const volatile Donation* vr = r;
+                p = vr->pair;
+                d = vr->depth;
+                for (int j = 0; j < kMaxN; ++j) s->chosen[j] = j < d ? vr->chosen[j] : -1;
+                rend = (int)((w >> 24) & 0xffffffu);
+                // the claim succeeds only while the record still holds these fields
+                don_claim(r, gen, lo, hi);
+            }
+        }
+        lo = __shfl_sync(kFull, lo, 0);
+        hi = __shfl_sync(kFull, hi, 0);
+        p = __shfl_sync(kFull, p, 0);
+        d = __shfl_sync(kFull, d, 0);
+        rend = __shfl_sync(kFull, rend, 0);
+        __syncwarp();
+        if (hi <= lo) return false;
+        if (p < 0 || p >= npairs) {
+            if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
+            __syncwarp();
+            return true;
+        }
+        const PairDesc pd = pairs[p];
+        P = pd.plan;
+        g = pd.g;
+        cap = pd.cap;
+        pair_idx = p;
+        bool ok = d >= 2 && d <= P->L;
+        for (int l = 0; l < d && ok; ++l) {
+            const int* nv;
+            int dv;
+            nbr(s->chosen[l], nv, dv);
+            ok = build_chain(l, nv, dv);
+        }
+        if (ok) {
+            start_level(d);
+            ok = s->end[d] == rend;
+        }
+        if (!ok) {
+            // the rebuilt loop differs from the published one: the slice is lost
+            if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
+            __syncwarp();
+            return true;
+        }
+        if (lane == 0) {
+            s->idx[d] = lo;
+            s->end[d] = hi;
+            s->dslot[d] = h;
+            s->dgen[d] = gen;
+            s->downer[d] = 0;
+        }
+        __syncwarp();
+        const __int128 acc = dfs_levels(d);
+        if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
+        return true;
+    }
+
+    // After the warp's own queues: helps published loops until every warp
+    // is done, or no record has had slices left for kIdleRounds scans in a
+    // row (so helpers never hold SMs that blocks not yet resident need).
+    __device__ void help_all(const PairDesc* pairs, int npairs, unsigned long long* out, unsigned total_warps) {
+        constexpr unsigned kIdleRounds = 4096;
+        unsigned idle = 0;
+        for (unsigned round = 0; round < (1u << 24) && idle < kIdleRounds; ++round) {
+            bool worked = false;
+            for (int base = 0; base < kDonSlots; base += 32) {
+                const int h = (int)((gw * 37 + base + lane) & (kDonSlots - 1));
+                const unsigned long long w = *(volatile unsigned long long*)&don->rec[h].word;
+                const bool live = (w & 0xffffffu) < ((w >> 24) & 0xffffffu);
+                unsigned m = __ballot_sync(kFull, live);
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int hj = __shfl_sync(kFull, h, j);
+                    const unsigned long long wj = __shfl_sync(kFull, w, j);
+                    if (help_one(pairs, npairs, out, hj, (unsigned)(wj >> 48))) worked = true;
+                }
+            }
+            if (worked) {
+                idle = 0;
+                continue;
+            }
+            if (*(volatile unsigned*)&don->finished >= total_warps) return;
+            ++idle;
+            __nanosleep(4000);
+        }
     }
 
     __device__ __int128 edge_task(int v0, int v1) {
@@ -654,7 +1052,9 @@ __global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restric
                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
                                                     long long scratch_per_warp, int chunk,
                                                     const unsigned long long* __restrict__ params,
-                                                    int leaf_on, int stage_cap,
+                                                    int leaf_on, int stage_cap, int pair_on,
+                                                    unsigned long long* __restrict__ pair_tables, int pair_log2,
+                                                    DonationArea* don, int split_min,
                                                     unsigned long long* __restrict__ stats) {
     // params[0] = stripes, params[1] = stripe (device memory, so a captured
     // graph can replay with new values)
@@ -668,27 +1068,38 @@ __global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restric
     w.stage = reinterpret_cast<int*>(reinterpret_cast<WarpState*>(smem_raw) + nwarps) + (size_t)wid * 2 * stage_cap;
     w.stage_cap = stage_cap;
     w.leaf_on = leaf_on;
+    w.pair_on = pair_on && pair_tables != nullptr;
+    w.pmask = (1u << pair_log2) - 1u;
+    w.ptab = pair_tables ? pair_tables + ((size_t)gw << pair_log2) : nullptr;
+    if (lane == 0) w.s->epoch = 0;  // the first pair sum clears the table
     w.scratch = scratch_all + gw * scratch_per_warp;
     w.lane = lane;
     w.bytes = 0;
+    w.don = don;
+    w.split_min = split_min;
+    w.gw = gw;
     for (int p = 0; p < npairs; ++p) {
         const PairDesc pd = pairs[p];
         w.P = pd.plan;
         w.g = pd.g;
         w.cap = pd.cap;
+        w.pair_idx = p;
         const int T = w.P->T;
         __int128 acc = 0;
         int cur_v0 = -1;
         unsigned cur_lo = 0, cur_hi = 0;
         for (;;) {
-            // chunk q of this stripe covers tasks [(q*stripes+stripe)*chunk, +chunk)
+            // Stripe `stripe` holds the tasks t with t mod stripes == stripe;
+            // grab q takes its members i in [q*chunk, q*chunk + chunk), i.e.
+            // tasks i*stripes + stripe (so the stripe does not depend on chunk).
             unsigned long long q = 0;
             if (lane == 0) q = atomicAdd(&cursors[p], 1ull);
             q = __shfl_sync(kFull, q, 0);
-            const unsigned long long t0 = (q * stripes + stripe) * (unsigned long long)chunk;
-            if (t0 >= pd.ntasks) break;
-            const unsigned long long t1 = min(t0 + (unsigned long long)chunk, pd.ntasks);
-            for (unsigned long long t = t0; t < t1; ++t) {
+            const unsigned long long i0 = q * (unsigned long long)chunk;
+            if (i0 * stripes + stripe >= pd.ntasks) break;
+            for (unsigned long long i = i0; i < i0 + (unsigned long long)chunk; ++i) {
+                const unsigned long long t = i * stripes + stripe;
+                if (t >= pd.ntasks) break;
                 if (T == 1) {
                     acc += w.root_task((int)t);
                     continue;
@@ -710,6 +1121,14 @@ __global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restric
             }
         }
         if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
+    }
+    if (don) {
+        if (lane == 0) {
+            __threadfence();
+            atomicAdd(&don->finished, 1u);
+        }
+        __syncwarp();
+        w.help_all(pairs, npairs, out, gridDim.x * (unsigned)nwarps);
     }
     if (kBytes && lane == 0 && w.bytes) atomicAdd(stats, w.bytes);
 }
@@ -1024,8 +1443,12 @@ struct LaunchSetup {
     size_t smem = 0;
     int chunk = 0;
     int leaf_on = 0;
+    int pair_on = 0;
+    int split_min = 0;
     bool count_bytes = false;
 };
+
+constexpr int kPairLog2 = 13;  // 8192-entry table per warp
 
 // Validates the pairs and sizes the launch from the current options.
 static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_plan* const* plans,
@@ -1056,7 +1479,19 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         nslots = std::max(nslots, p->host.nslots);
     }
     ls.wpb = (int)o.warps_per_block;
-    ls.blocks = (long long)c->num_sms * o.blocks_per_sm;
+    ls.stage_cap = (int)o.stage_max;
+    ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)ls.stage_cap * ls.wpb;
+    ls.count_bytes = o.count_bytes != 0;
+    const void* kfn = ls.count_bytes ? (const void*)match_kernel<true> : (const void*)match_kernel<false>;
+    GPM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
+    // a persistent grid: no more blocks than can be resident at once
+    int occ = 0;
+    GPM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kfn, ls.wpb * 32, ls.smem));
+    if (occ < 1) {
+        set_error("launch shape does not fit an SM: %d warps per block, %zu bytes of shared memory", ls.wpb, ls.smem);
+        return GPM_ERR_INVALID_ARG;
+    }
+    ls.blocks = (long long)c->num_sms * std::min<long long>(o.blocks_per_sm, occ);
     ls.per_warp = (long long)nslots * cap;
     // shrink the grid when the per-warp scratch would not fit in free memory
     size_t free_b = 0, total_b = 0;
@@ -1066,33 +1501,64 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         ls.blocks = (ls.blocks + 1) / 2;
     const int alpha4[3] = {(int)o.merge_alpha4[0], (int)o.merge_alpha4[1], (int)o.merge_alpha4[2]};
     GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, c->stream));
-    ls.stage_cap = (int)o.stage_max;
-    ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)ls.stage_cap * ls.wpb;
     ls.chunk = (int)o.chunk;
     ls.leaf_on = (int)o.leaf_batch;
-    ls.count_bytes = o.count_bytes != 0;
-    if (ls.count_bytes)
-        GPM_CK(cudaFuncSetAttribute(match_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
-    else
-        GPM_CK(cudaFuncSetAttribute(match_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
+    ls.pair_on = 0;
+    if (o.pair_leaf) {
+        bool any = false;
+        for (int i = 0; i < n; ++i) any |= plans[i]->host.pair_ok && graphs[i]->v_cnt <= (1 << 24);
+        ls.pair_on = any ? 1 : 0;
+    }
+    ls.split_min = (int)o.split;
     return GPM_OK;
 }
 
 // small device words of a launch: cursors[n], out[2n], stats[2], params[2]
 static size_t small_words(int n) { return (size_t)n * 3 + 4; }
 
-static void enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d_pairs, unsigned long long* d_small,
-                          int* scratch, cudaStream_t st) {
+// Scratch of a launch: per-warp set slots, per-warp pair tables, then the
+// donation records (zeroed before every launch).
+struct ScratchLayout {
+    size_t tables = 0, donation = 0, total = 0;
+};
+
+static ScratchLayout scratch_layout(const LaunchSetup& ls) {
+    const size_t warps = (size_t)ls.blocks * ls.wpb;
+    ScratchLayout s;
+    size_t b = warps * (size_t)ls.per_warp * sizeof(int);
+    b = (b + 255) & ~(size_t)255;
+    s.tables = b;
+    if (ls.pair_on) b += warps * ((size_t)1 << kPairLog2) * sizeof(unsigned long long);
+    s.donation = b;
+    if (ls.split_min > 0) b += sizeof(DonationArea);
+    s.total = std::max<size_t>(b, 1);
+    return s;
+}
+
+static size_t scratch_bytes(const LaunchSetup& ls) { return scratch_layout(ls).total; }
+
+static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d_pairs,
+                                 unsigned long long* d_small, int* scratch, cudaStream_t st) {
     unsigned long long* cursors = d_small;
     unsigned long long* out = cursors + n;
     unsigned long long* stats = out + 2 * n;
     const unsigned long long* params = stats + 2;
+    const ScratchLayout lay = scratch_layout(ls);
+    unsigned long long* tables = ls.pair_on ? (unsigned long long*)((char*)scratch + lay.tables) : nullptr;
+    DonationArea* don = ls.split_min > 0 ? (DonationArea*)((char*)scratch + lay.donation) : nullptr;
+    if (don) {
+        const cudaError_t e = cudaMemsetAsync(don, 0, sizeof(DonationArea), st);
+        if (e != cudaSuccess) return e;
+    }
     if (ls.count_bytes)
         match_kernel<true><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
-            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, stats);
+            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
+            tables, kPairLog2, don, ls.split_min, stats);
     else
         match_kernel<false><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
-            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, stats);
+            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
+            tables, kPairLog2, don, ls.split_min, stats);
+    return cudaGetLastError();
 }
 
 // Launches the matcher over n pairs and leaves raw 128-bit sums in host_raw
@@ -1102,7 +1568,7 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     LaunchSetup ls;
     int rc = prepare_pairs(c, n, graphs, plans, c->scratch_bytes, ls);
     if (rc) return rc;
-    rc = ensure_scratch(c, (size_t)ls.blocks * ls.wpb * ls.per_warp * sizeof(int));
+    rc = ensure_scratch(c, scratch_bytes(ls));
     if (rc) return rc;
     DevBuf d_pairs, d_small;
     GPM_CK(cudaMalloc(&d_pairs.p, sizeof(PairDesc) * n));
@@ -1115,8 +1581,7 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     GPM_CK(cudaMemcpyAsync(d_pairs.p, ls.descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
     GPM_CK(cudaMemcpyAsync(d_small.p, init.data(), words * sizeof(unsigned long long), cudaMemcpyHostToDevice, st));
     GPM_CK(cudaEventRecord(c->ev0, st));
-    enqueue_match(ls, n, (const PairDesc*)d_pairs.p, (unsigned long long*)d_small.p, (int*)c->scratch, st);
-    GPM_CK(cudaGetLastError());
+    GPM_CK(enqueue_match(ls, n, (const PairDesc*)d_pairs.p, (unsigned long long*)d_small.p, (int*)c->scratch, st));
     GPM_CK(cudaEventRecord(c->ev1, st));
     std::vector<unsigned long long> raw(2 * n + 2);
     GPM_CK(cudaMemcpyAsync(raw.data(), (unsigned long long*)d_small.p + n, sizeof(unsigned long long) * (2 * n + 2),
@@ -1416,7 +1881,7 @@ static int exec_build(DeviceCtx* c, gpm_batch_exec* e, gpm_graph* const* graphs)
     GPM_CK(cudaMalloc(&e->d_pairs, sizeof(PairDesc) * n));
     GPM_CK(cudaMalloc(&e->d_small, words * sizeof(unsigned long long)));
     GPM_CK(cudaMallocHost(&e->h_small, (2 * (size_t)n + 4) * sizeof(unsigned long long)));
-    GPM_CK(cudaMalloc(&e->scratch, std::max<size_t>(1, (size_t)e->ls.blocks * e->ls.wpb * e->ls.per_warp * sizeof(int))));
+    GPM_CK(cudaMalloc(&e->scratch, scratch_bytes(e->ls)));
     cudaStream_t st = c->stream;
     GPM_CK(cudaMemcpyAsync(e->d_pairs, e->ls.descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
     GPM_CK(cudaStreamSynchronize(st));
@@ -1425,11 +1890,12 @@ static int exec_build(DeviceCtx* c, gpm_batch_exec* e, gpm_graph* const* graphs)
     GPM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaMemcpyAsync(d_params, h_params, 2 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(e->d_small, 0, (3 * (size_t)n + 2) * sizeof(unsigned long long), st);
-    enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, st);
+    const cudaError_t qe = enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, st);
     cudaMemcpyAsync(e->h_small, e->d_small + n, (2 * (size_t)n + 2) * sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, st);
     cudaGraph_t g = nullptr;
     cudaError_t err = cudaStreamEndCapture(st, &g);
+    if (err == cudaSuccess && qe != cudaSuccess) err = qe;
     if (err != cudaSuccess) {
         set_error("CUDA graph capture failed: %s", cudaGetErrorString(err));
         if (g) cudaGraphDestroy(g);

@@ -22,7 +22,8 @@ struct Options {
     int64_t timeout_ms = 2000;  // bounded device waits
     int64_t stage_max = 1024;   // largest fixed set staged in shared memory (ints)
     int64_t leaf_batch = 1;     // 1: batched deepest level where the plan allows
-    int64_t split = 0;          // reserved: hub splitting width
+    int64_t pair_leaf = 0;      // 1: pair sums over the last two levels where the plan allows
+    int64_t split = 64;         // loops this long (depth >= 2) are shared with idle warps; 0 = off
     int64_t stripes = 1;        // a launch covers chunks q*stripes + stripe only
     int64_t stripe = 0;
     int64_t raw_sums = 0;       // 1: return undivided 128-bit sums
@@ -60,6 +61,13 @@ struct DevPlan {
     int leaf_sa, leaf_sb;        // prefix ids of the tail's loop sets (kLeafIep2)
     int leaf_ka, leaf_kb;        // 0 fixed, 1 N(v), 2 father ∩ N(v)
     int leaf_cab, leaf_cx;       // group coefficients of |a|*|b| and |a ∩ b|
+    // Pair sum over the last two loops (kLeafCount plans whose counted set is
+    // N(v_{L-1}) ∩ N(v_L), whose level-L candidates and bound do not depend
+    // on v_{L-1}, and whose tail bound is fixed before L-1): the count over
+    // candidate pairs equals sum_x a_x * b_x - c_x, where a_x / b_x count the
+    // level L-1 / L candidates adjacent to x and c_x the candidates of both.
+    int pair_ok;
+    int pair_pad_;
     long long redundancy;
     int loop_set[kMaxN];
     unsigned rmask[kMaxN];         // depth d stays below min(chosen[j]) for bits j

@@ -51,6 +51,7 @@ SIGNATURES = {
     "gpm_pattern_multiplicity": (I32, [I32, P, PI64]),
     "gpm_schedule_build": (I32, [I32, P, I32, I32, I32, I64, U64, I64, P, I32, PI32, PI32]),
     "gpm_schedule_analyze": (I32, [P, I32, PI32]),
+    "gpm_plan_info": (I32, [P, I32, P, I32]),
     "gpm_schedule_candidates": (I32, [I32, P, I32, I32, I64, U64, I64, P, P, P, P, I32, PI32]),
     "gpm_schedule_from_order": (I32, [I32, P, P, I32, P, I32, I32, P, I32, PI32, PI32]),
     "gpm_plan_create": (I32, [P, I32, C.POINTER(P)]),

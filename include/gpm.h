@@ -156,6 +156,14 @@ GPM_API int gpm_schedule_from_order(int32_t n, const int32_t* adj, const int32_t
  * never on the degree-relabelled copy, so results equal the reference's. */
 GPM_API int gpm_schedule_analyze(const int64_t* tables, int32_t n_words, int32_t* label_sensitive);
 
+/* How the engine will evaluate a schedule: info[0] tail depth T, [1]
+ * deepest loop level L, [2] inclusion–exclusion length k, [3] leaf mode of
+ * level L (0 candidate by candidate, 1 batched count, 2 batched two-loop
+ * inclusion–exclusion), [4] 1 when the last two loops can be summed in
+ * pairs (option "pair_leaf"), [5] label-sensitive (see
+ * gpm_schedule_analyze).  cap >= 6. */
+GPM_API int gpm_plan_info(const int64_t* tables, int32_t n_words, int32_t* info, int32_t cap);
+
 /* Compiles schedule tables (layout of gpm_schedule_build) into a device
  * plan: per-depth candidate lists, restriction bounds, prefix-set slots and
  * the inclusion-exclusion groups.  Replaces the table walks of
@@ -229,12 +237,15 @@ GPM_API int gpm_mlp_train(gpm_mlp* m, const float* X, const float* T, int32_t n_
 
 /* Engine knobs (counts never depend on them):
  *   "warps_per_block", "blocks_per_sm", "chunk" (work-queue grab size),
- *   "split" (first-level candidates per task for hub roots),
+ *   "split" (a loop at depth >= 2 with at least this many candidates is
+ *   published so that idle warps take slices of it; 0 = off),
  *   "stage_max" (largest father set staged in shared memory),
+ *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan allows),
+ *   "merge_alpha4_small"/"_mid"/"_large" (merge vs search per length bucket),
  *   "timeout_ms" (bounded waits),
- *   "stripes"/"stripe" (a launch covers only work chunks q*stripes+stripe:
- *   the first-level tasks split into `stripes` interleaved parts, e.g. one
- *   per GPU or per bounded step), "raw_sums" (1: outputs are the undivided
+ *   "stripes"/"stripe" (a launch covers only the first-level tasks t with
+ *   t mod stripes == stripe: the tasks split into `stripes` interleaved
+ *   parts, e.g. one per GPU or per bounded step), "raw_sums" (1: outputs are the undivided
  *   signed 128-bit sums, to be added over stripes and then divided by the
  *   schedule's redundancy; required when stripes > 1),
  *   "count_bytes" (1: count algorithmic bytes).  Returns

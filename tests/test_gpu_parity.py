@@ -249,3 +249,70 @@ def test_uneven_multi_graph_batch(engine, oracle):
         scheds.append(gp.Schedule(motifs[m], 1, 1, True, g.v_cnt, g.e_cnt, oracle.triangles(g)))
     got = gp.batch_count(graphs, scheds)
     assert got == [oracle.count(g, s) for g, s in zip(graphs, scheds)]
+
+
+def _with_options(opts: dict, fn):
+    old = {k: gp.get_option(k) for k in opts}
+    for k, v in opts.items():
+        gp.set_option(k, v)
+    try:
+        return fn()
+    finally:
+        for k, v in old.items():
+            gp.set_option(k, v)
+
+
+def test_loop_donation_matches_oracle(engine, oracle):
+    # skewed graph: hub loops are published and sliced by idle warps; with
+    # split=1 every loop at depth >= 2 is shared, the most racy setting
+    g = gp.rmat(11, 16, 0.57, 0.19, 0.19, 31)
+    tri = g.triangle_counting_mt()
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
+    scheds += [gp.Schedule(p, 1, 1, False, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()[8::4]]
+    want = [oracle.count(g, s) for s in scheds]
+    pairs = [g] * len(scheds)
+    assert _with_options({"split": 0}, lambda: gp.batch_count(pairs, scheds)) == want
+    for split in (1, 3, 64):
+        for leaf in (0, 1):
+            got = _with_options({"split": split, "leaf_batch": leaf}, lambda: gp.batch_count(pairs, scheds))
+            assert got == want, (split, leaf)
+    # few warps, many slices each
+    got = _with_options({"split": 2, "warps_per_block": 4, "blocks_per_sm": 1}, lambda: gp.batch_count(pairs, scheds))
+    assert got == want
+
+
+def test_loop_donation_six_vertex(engine, oracle):
+    g = gp.chung_lu(600, 10.0, 2.1, 150, 9)
+    tri = oracle.triangles(g)
+    pats = gp.MotifGenerator(6).generate()[::9]
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in pats]
+    want = [oracle.count(g, s) for s in scheds]
+    got = _with_options({"split": 1}, lambda: gp.batch_count([g] * len(scheds), scheds))
+    assert got == want
+
+
+def test_pair_sum_leaf_matches_oracle(engine, oracle):
+    # the pair-sum leaf (sum_x a_x b_x - c_x) against the per-candidate path:
+    # a sparse graph whose tables fit, and a dense one whose hub tasks fall
+    # back to the loops
+    for g in (gp.chung_lu(3000, 8.0, 2.5, 100, 12), gp.rmat(10, 24, 0.57, 0.19, 0.19, 13)):
+        tri = oracle.triangles(g)
+        scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
+        scheds = [s for s in scheds if s.plan_info()["pair_ok"]]
+        assert scheds, "no plan takes the pair-sum leaf"
+        want = [oracle.count(g, s) for s in scheds]
+        for split in (0, 1):
+            got = _with_options({"pair_leaf": 1, "split": split}, lambda: gp.batch_count([g] * len(scheds), scheds))
+            assert got == want, split
+
+
+def test_stripes_do_not_depend_on_chunk(engine):
+    g = gp.rmat(11, 10, 0.57, 0.19, 0.19, 8)
+    tri = g.triangle_counting_mt()
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()[::3]]
+    pairs = [g] * len(scheds)
+    runs = []
+    for chunk in (1, 8, 64):
+        opts = {"raw_sums": 1, "stripes": 8, "stripe": 5, "chunk": chunk}
+        runs.append(_with_options(opts, lambda: gp.batch_count(pairs, scheds)))
+    assert runs[0] == runs[1] == runs[2]
