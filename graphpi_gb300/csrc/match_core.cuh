@@ -1,0 +1,1139 @@
+// Device core of the matcher: the per-warp DFS (WarpCtx) and the persistent
+// match_kernel, included by gpm_device.cu inside namespace gpm.
+//
+// With GPM_EMU defined, the same source compiles as host C++ against the
+// warp emulator of the tests (tests/emu/warp_emu.h: 32 host threads per warp,
+// lock-step warp intrinsics), so the kernel's indexing and its donation
+// protocol can be checked on the CPU under AddressSanitizer.
+#pragma once
+constexpr unsigned kFull = 0xffffffffu;
+
+// Internal-check record: the first kernel that detects an impossible state
+// (a merge window that does not advance, an id outside the graph) writes a
+// code and a few values here and skips the work; the host reports it.
+// [0] code, [1..7] values.
+constexpr int kErrMergeStall = 1, kErrBadVertex = 2, kErrLoopIndex = 5, kErrSetSize = 6;
+__device__ unsigned long long g_check[8];
+
+__device__ __noinline__ void record_check(int code, long long a, long long b, long long c, long long d, long long e,
+                                          long long f) {
+    if (atomicCAS(&g_check[0], 0ull, (unsigned long long)code) == 0ull) {
+        g_check[1] = (unsigned long long)a;
+        g_check[2] = (unsigned long long)b;
+        g_check[3] = (unsigned long long)c;
+        g_check[4] = (unsigned long long)d;
+        g_check[5] = (unsigned long long)e;
+        g_check[6] = (unsigned long long)f;
+        __threadfence();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// device building blocks
+
+struct GraphView {
+    const unsigned* __restrict__ rowptr;
+    const int* __restrict__ col;
+    int v_cnt;
+    int pad_;
+    unsigned long long e_cnt;
+};
+
+struct PairDesc {
+    GraphView g;
+    const DevPlan* plan;
+    unsigned long long ntasks;  // v_cnt when the tail starts at depth 1, else e_cnt
+    int cap;                    // scratch ints per slot for this graph
+    int pad_;
+};
+
+struct WarpState {
+    int chosen[kMaxN];
+    int idx[kMaxN];
+    int end[kMaxN];
+    int len[kMaxPrefix];
+    const int* ptr[kMaxPrefix];
+    const int* lp[kMaxN];
+    int blockval[kMaxBlocks];
+    int leafcnt[3][32];  // per-candidate counters of a leaf batch
+    unsigned epoch;      // tag of the live entries of this warp's pair-sum table
+    int dslot[kMaxN];    // donation record the loop of depth d draws from (-1: none)
+    unsigned dgen[kMaxN];
+    int downer[kMaxN];   // 1: this warp published that record
+};
+
+// Work donation (hub splitting).  A warp whose loop at depth d >= 2 has at
+// least `split` candidates publishes the loop as a record: the pair, d and
+// chosen[0, d).  From then on the owner and any warp that has finished its
+// own queues take slices [next, next + s) of the loop by compare-and-swap on
+// the record's word; a helper rebuilds the prefix sets of chosen[0, d) and
+// adds what it counts to the pair's sum.  Nothing waits on a record: a warp
+// that finds no free slot runs its loop alone, a claim either succeeds or
+// sees the loop exhausted, and only the owner frees a slot, after the last
+// slice has been taken (helpers keep their own copies of what they need).
+constexpr int kDonSlots = 1024;
+constexpr int kErrDonation = 4;
+
+struct Donation {
+    unsigned long long word;  // generation (16 bits) | end (24) | next (24)
+    int pair;
+    int depth;
+    int chosen[kMaxN];
+    int pad_[4];
+};
+static_assert(sizeof(Donation) == 64, "one record per 64 bytes");
+
+struct DonationArea {
+    Donation rec[kDonSlots];
+    unsigned busy[kDonSlots];  // 1 while a record's owner holds the slot
+    unsigned finished;         // warps done with their own queues
+    unsigned pad_[3];
+};
+
+__device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned end, unsigned next) {
+    return ((unsigned long long)(gen & 0xffffu) << 48) | ((unsigned long long)(end & 0xffffffu) << 24) |
+           (unsigned long long)(next & 0xffffffu);
+}
+
+// Takes the next slice of record r (generation gen); lo == hi when the loop
+// is exhausted or the slot holds another generation.  Lock-free: a failed
+// compare-and-swap means another warp took a slice, so the retries are
+// bounded by the loop length (< 2^24).
+__device__ void don_claim(Donation* r, unsigned gen, int& lo, int& hi) {
+    lo = hi = 0;
+    unsigned long long w = *(volatile unsigned long long*)&r->word;
+    for (int tries = 0; tries < (1 << 25); ++tries) {
+        if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
+        const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
+        if (next >= end) return;
+        const unsigned take = min(64u, max(1u, (end - next) >> 5));
+        const unsigned long long got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
+        if (got == w) {
+            lo = (int)next;
+            hi = (int)(next + take);
+            return;
+        }
+        w = got;
+    }
+    record_check(kErrDonation, gen, (long long)w, 0, 0, 0, 0);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+#ifdef GPM_EMU
+    return (1u << (threadIdx.x & 31u)) - 1u;
+#else
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+#endif
+}
+
+// first index i in a[0, n) with a[i] >= x (all lanes search the same key)
+__device__ __forceinline__ int lower_bound_u(const int* a, int n, int x) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (a[mid] < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Merge variant: both lists advance through 32-wide coalesced windows; each
+// lane locates its A element in the B window with a 5-step shuffle search.
+// Elements of A no larger than the last B of the window are resolved and
+// consumed, likewise for B, so each step consumes a full window of at least
+// one list.  Found elements are compacted in order (kStore) or counted minus
+// the chosen vertices.
+template <bool kStore>
+__device__ int warp_merge(const int* A, int na, const int* B, int nb, int* out, const int* chosen, int nch,
+                          int lane) {
+    int i = 0, j = 0, acc = 0;
+    while (i < na && j < nb) {
+        const int a = (i + lane < na) ? A[i + lane] : INT_MAX;
+        const int b = (j + lane < nb) ? B[j + lane] : INT_MAX;
+        int pos = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int bv = __shfl_sync(kFull, b, pos + step - 1);
+            if (bv < a) pos += step;
+        }
+        // every lane must execute the shuffle (no short-circuit around it)
+        const int bp = __shfl_sync(kFull, b, pos);
+        bool found = (a != INT_MAX) && (bp == a);
+        if (!kStore && found)
+            for (int q = 0; q < nch; ++q)
+                if (chosen[q] == a) found = false;
+        const unsigned fm = __ballot_sync(kFull, found);
+        if (kStore && found) out[acc + __popc(fm & lanemask_lt())] = a;
+        acc += __popc(fm);
+        const int amax = __shfl_sync(kFull, a, 31), bmax = __shfl_sync(kFull, b, 31);
+        const int di = __popc(__ballot_sync(kFull, a <= bmax));
+        const int dj = __popc(__ballot_sync(kFull, b <= amax));
+        if (di == 0 && dj == 0) {
+            // only possible when a window is not sorted: record and stop
+            const int a0 = __shfl_sync(kFull, a, 0);
+            if (lane == 0) record_check(kErrMergeStall, na, nb, i, j, a0, bmax);
+            break;
+        }
+        i += di;
+        j += dj;
+    }
+    if (kStore) __syncwarp();
+    return acc;
+}
+
+// Merge when both lists are of similar length: a binary-search round costs
+// about log2(nb) dependent loads for 32 elements of the short list, a merge
+// step one coalesced load per list for at least 32 elements.
+// alpha4 = 4 x the weight of a binary-search round, per bucket of the longer
+// list's length (< 256, < 8192, larger); the autotuner sets them.
+__constant__ int c_merge_alpha4[3] = {4, 4, 4};
+
+__device__ __forceinline__ bool prefer_merge(int na, int nb) {
+    const int lg = 32 - __clz(nb | 1);
+    const int a4 = c_merge_alpha4[nb < 256 ? 0 : (nb < 8192 ? 1 : 2)];
+    return (long long)na * lg * a4 >= 4ll * (long long)(na + nb);
+}
+
+// A ∩ B written sorted to out; returns its size.
+__device__ int isect_store(const int* A, int na, const int* B, int nb, int* out, int lane) {
+    if (na > nb) {
+        const int* t = A; A = B; B = t;
+        int u = na; na = nb; nb = u;
+    }
+    if (prefer_merge(na, nb)) return warp_merge<true>(A, na, B, nb, out, nullptr, 0, lane);
+    int written = 0, lo = 0;
+    for (int base = 0; base < na; base += 32) {
+        const int i = base + lane;
+        const bool valid = i < na;
+        const int x = valid ? A[i] : INT_MAX;
+        int l = lo, h = nb;
+        while (l < h) {
+            int m = (l + h) >> 1;
+            if (B[m] < x) l = m + 1;
+            else h = m;
+        }
+        const bool found = valid && l < nb && B[l] == x;
+        const unsigned mask = __ballot_sync(kFull, found);
+        if (found) out[written + __popc(mask & lanemask_lt())] = x;
+        written += __popc(mask);
+        lo = __shfl_sync(kFull, l, 31);
+    }
+    __syncwarp();
+    return written;
+}
+
+// |A ∩ B ∩ [0, bound) \ chosen[0, nch)|
+__device__ int isect_count(const int* A, int na, const int* B, int nb, int bound, const int* chosen, int nch,
+                           int lane) {
+    na = lower_bound_u(A, na, bound);
+    nb = lower_bound_u(B, nb, bound);
+    if (na > nb) {
+        const int* t = A; A = B; B = t;
+        int u = na; na = nb; nb = u;
+    }
+    if (prefer_merge(na, nb)) return warp_merge<false>(A, na, B, nb, nullptr, chosen, nch, lane);
+    int cnt = 0, lo = 0;
+    for (int base = 0; base < na; base += 32) {
+        const int i = base + lane;
+        const bool valid = i < na;
+        const int x = valid ? A[i] : INT_MAX;
+        int l = lo, h = nb;
+        while (l < h) {
+            int m = (l + h) >> 1;
+            if (B[m] < x) l = m + 1;
+            else h = m;
+        }
+        bool found = valid && l < nb && B[l] == x;
+        if (found)
+            for (int j = 0; j < nch; ++j)
+                if (chosen[j] == x) found = false;
+        cnt += __popc(__ballot_sync(kFull, found));
+        lo = __shfl_sync(kFull, l, 31);
+    }
+    return cnt;
+}
+
+// |S[0, len) \ chosen[0, nch)|  (VertexSet::unorderd_subtraction_size,
+// src/vertex_set.cpp:196-209)
+__device__ __forceinline__ int count_outside(const int* S, int len, const int* chosen, int nch, int lane) {
+    bool in = false;
+    if (lane < nch) {
+        const int c = chosen[lane];
+        const int p = lower_bound_u(S, len, c);
+        in = p < len && S[p] == c;
+    }
+    return len - __popc(__ballot_sync(kFull, in));
+}
+
+__device__ __forceinline__ void add128(unsigned long long* o, __int128 v) {
+    const unsigned long long lo = (unsigned long long)v;
+    const unsigned long long hi = (unsigned long long)(v >> 64);
+    const unsigned long long old = atomicAdd(o, lo);
+    const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
+    if (hi + carry) atomicAdd(o + 1, hi + carry);
+}
+
+// Pair-sum table entries: epoch (16 bits) | vertex (24 bits) | count (24 bits).
+// A slot whose epoch differs from the warp's current one is empty.
+__device__ __forceinline__ unsigned long long pair_word(unsigned epoch, int x, unsigned cnt) {
+    return ((unsigned long long)(epoch & 0xffffu) << 48) | ((unsigned long long)(x & 0xffffff) << 24) | cnt;
+}
+
+__device__ __forceinline__ unsigned pair_slot(int x, unsigned mask) { return ((unsigned)x * 2654435761u) >> 7 & mask; }
+
+// adds one to x's count; false when the table is full (never at load <= 1/2)
+__device__ bool pair_add(unsigned long long* T, unsigned mask, unsigned epoch, int x) {
+    unsigned slot = pair_slot(x, mask);
+    for (unsigned probes = 0; probes <= mask; ++probes) {
+        unsigned long long old = T[slot];
+        for (;;) {
+            const bool live = (unsigned)(old >> 48) == (epoch & 0xffffu);
+            if (live && (int)((old >> 24) & 0xffffff) == x) {
+                const unsigned long long got = atomicCAS(&T[slot], old, old + 1);
+                if (got == old) return true;
+                old = got;
+                continue;
+            }
+            if (!live) {
+                const unsigned long long got = atomicCAS(&T[slot], old, pair_word(epoch, x, 1));
+                if (got == old) return true;
+                old = got;
+                continue;
+            }
+            break;  // live entry of another vertex: next slot
+        }
+        slot = (slot + 1) & mask;
+    }
+    return false;
+}
+
+__device__ unsigned pair_get(const unsigned long long* T, unsigned mask, unsigned epoch, int x) {
+    unsigned slot = pair_slot(x, mask);
+    for (unsigned probes = 0; probes <= mask; ++probes) {
+        const unsigned long long w = T[slot];
+        if ((unsigned)(w >> 48) != (epoch & 0xffffu)) return 0;
+        if ((int)((w >> 24) & 0xffffff) == x) return (unsigned)(w & 0xffffff);
+        slot = (slot + 1) & mask;
+    }
+    return 0;
+}
+
+// x in sorted a[0, n) (per-lane search)
+__device__ __forceinline__ bool contains(const int* a, int n, int x) {
+    const int p = lower_bound_u(a, n, x);
+    return p < n && a[p] == x;
+}
+
+template <bool kBytes>
+struct WarpCtx {
+    WarpState* s;
+    const DevPlan* __restrict__ P;
+    GraphView g;
+    int* scratch;
+    int cap;
+    int lane;
+    int leaf_on;
+    int* stage;      // 2 * stage_cap ints of this warp's shared memory
+    int stage_cap;
+    int pair_on;
+    unsigned long long* ptab;  // this warp's pair-sum table (pmask + 1 words)
+    unsigned pmask;
+    DonationArea* don;         // null: no donation
+    int split_min;             // smallest loop that is donated
+    int pair_idx;              // pair whose work is running
+    long long gw;              // global warp index
+    unsigned long long bytes;
+
+    // copies a fixed set into shared-memory region r when it fits
+    __device__ const int* stage_set(const int* p, int n, int r) {
+        if (n > stage_cap || n <= 0) return p;
+        int* dst = stage + r * stage_cap;
+        for (int i = lane; i < n; i += 32) dst[i] = p[i];
+        __syncwarp();
+        return dst;
+    }
+
+    // Exclusive scan of len over the warp; returns the total.
+    __device__ __forceinline__ int warp_scan(int len, int& pre) const {
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += t;
+        }
+        pre = incl - len;
+        return __shfl_sync(kFull, incl, 31);
+    }
+
+    // owner lane of flat element e: the largest lane c with pre_c <= e
+    __device__ __forceinline__ int owner(int pre, int e) const {
+        int c = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int q = c + step;
+            const int pq = __shfl_sync(kFull, pre, q & 31);
+            if (q < 32 && pq <= e) c = q;
+        }
+        return c;
+    }
+
+    __device__ __forceinline__ bool chosen_before(int x, int L) const {
+        bool hit = false;
+        for (int q = 0; q < L; ++q) hit |= s->chosen[q] == x;
+        return hit;
+    }
+
+    // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
+    // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
+    // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
+    // (and does nothing) when B's neighbour lists would fill the table more
+    // than half: the caller then runs the level normally.
+    __device__ bool pair_level(__int128& out) {
+        const int L1 = P->L - 1;
+        const int T = P->T;
+        const int* candA = s->lp[L1];
+        const int na = s->end[L1];
+        const int sb = P->loop_set[P->L];
+        const int* candB = s->ptr[sb];
+        const int nb = lower_bound_u(candB, s->len[sb], bound_of(P->L));
+        const int bnd = bound_of(T);
+        // size of B's neighbour lists below the bound
+        long long mb = 0;
+        for (int base = 0; base < nb; base += 32) {
+            const int j = base + lane;
+            int len = 0;
+            if (j < nb) {
+                const int w = candB[j];
+                if (!chosen_before(w, L1)) {
+                    const unsigned st = g.rowptr[w];
+                    len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
+                }
+            }
+            int pre;
+            mb += warp_scan(len, pre);
+        }
+        if (mb * 2 > (long long)pmask + 1) return false;
+        if (lane == 0) {
+            s->epoch = (s->epoch + 1) & 0xffffu;
+            if (s->epoch == 0) s->epoch = 1;
+        }
+        __syncwarp();
+        const unsigned ep = s->epoch;
+        if (ep == 1) {  // fresh cycle of tags: clear the table
+            for (unsigned i = lane; i <= pmask; i += 32) ptab[i] = 0ull;
+            __syncwarp();
+        }
+        long long sum = 0;
+        // phase 1 (B -> counts) and phase 2 (A -> sum of counts)
+        for (int phase = 0; phase < 2; ++phase) {
+            const int* cand = phase == 0 ? candB : candA;
+            const int nc = phase == 0 ? nb : na;
+            for (int base = 0; base < nc; base += 32) {
+                const int j = base + lane;
+                unsigned st = 0;
+                int len = 0;
+                if (j < nc) {
+                    const int v = cand[j];
+                    if (!chosen_before(v, L1)) {
+                        st = g.rowptr[v];
+                        len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
+                        if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
+                    }
+                }
+                int pre;
+                const int M = warp_scan(len, pre);
+                for (int eb = 0; eb < M; eb += 32) {
+                    const int e = eb + lane;
+                    const int c = owner(pre, e);
+                    const unsigned stc = __shfl_sync(kFull, st, c);
+                    const int prc = __shfl_sync(kFull, pre, c);
+                    if (e < M) {
+                        const int x = g.col[stc + (e - prc)];
+                        if (!chosen_before(x, L1)) {
+                            if (phase == 0) {
+                                if (!pair_add(ptab, pmask, ep, x)) record_check(3, x, mb, pmask, 0, 0, 0);
+                            } else {
+                                sum += pair_get(ptab, pmask, ep, x);
+                            }
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        // c term: v in both candidate lists pairs with itself
+        for (int base = 0; base < na; base += 32) {
+            const int j = base + lane;
+            if (j < na) {
+                const int v = candA[j];
+                if (!chosen_before(v, L1) && contains(candB, nb, v)) {
+                    const unsigned st = g.rowptr[v];
+                    const int* nv = g.col + st;
+                    const int len = lower_bound_u(nv, (int)(g.rowptr[v + 1] - st), bnd);
+                    int in = 0;
+                    for (int q = 0; q < L1; ++q) in += contains(nv, len, s->chosen[q]) ? 1 : 0;
+                    sum -= (long long)(len - in);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+        out = lane == 0 ? (__int128)sum : (__int128)0;
+        return true;
+    }
+
+    // All candidates of level L at once (the plan's leaf_kind says how the
+    // tail reads N(v)); chosen[0, L) and the level's loop list are set.
+    __device__ __int128 leaf_batch() {
+        const int L = P->L, T = P->T;
+        const int* cand = s->lp[L];
+        const int ncand = s->end[L];
+        long long total = 0;
+        if (P->leaf_kind == kLeafCount) {
+            // bound of the last loop: restrictions on depths < L are fixed
+            const unsigned m = P->rmask[T];
+            int bfix = g.v_cnt;
+            for (int j = 0; j < L; ++j)
+                if (m >> j & 1) bfix = min(bfix, s->chosen[j]);
+            const bool by_v = (m >> L) & 1;
+            const int* F = nullptr;
+            int nf = 0, lim = bfix;
+            if (P->leaf_fa >= 0) {
+                nf = lower_bound_u(s->ptr[P->leaf_fa], s->len[P->leaf_fa], bfix);
+                if (nf == 0) return 0;
+                F = stage_set(s->ptr[P->leaf_fa], nf, 0);
+                lim = min(bfix, F[nf - 1] + 1);
+            }
+            for (int base = 0; base < ncand; base += 32) {
+                const int j = base + lane;
+                bool ok = j < ncand;
+                const int v = ok ? cand[j] : 0;
+                if (ok) ok = !chosen_before(v, L);
+                unsigned st = 0;
+                int len = 0;
+                if (ok) {
+                    st = g.rowptr[v];
+                    const int dv = (int)(g.rowptr[v + 1] - st);
+                    len = lower_bound_u(g.col + st, dv, by_v ? min(lim, v) : lim);
+                    if (kBytes) bytes += 4ull * (unsigned long long)(s->len[P->leaf_fa >= 0 ? P->leaf_fa : 0] * (P->leaf_fa >= 0) + dv) + 8;
+                }
+                int pre;
+                const int M = warp_scan(len, pre);
+                for (int eb = 0; eb < M; eb += 32) {
+                    const int e = eb + lane;
+                    const int c = owner(pre, e);
+                    const unsigned stc = __shfl_sync(kFull, st, c);
+                    const int prc = __shfl_sync(kFull, pre, c);
+                    bool hit = false;
+                    if (e < M) {
+                        const int x = g.col[stc + (e - prc)];
+                        hit = !chosen_before(x, L);
+                        if (hit && F) hit = contains(F, nf, x);
+                    }
+                    total += __popc(__ballot_sync(kFull, hit));
+                }
+            }
+            return lane == 0 ? (__int128)total : (__int128)0;
+        }
+        // ---- two-loop inclusion–exclusion tail ----
+        const int sa = P->leaf_sa, sb = P->leaf_sb, ka = P->leaf_ka, kb = P->leaf_kb;
+        const bool same = sa == sb, both_fixed = ka == 0 && kb == 0;
+        const int* Pa = nullptr;
+        const int* Pb = nullptr;
+        int na = 0, nb = 0;
+        if (P->leaf_fa >= 0) {
+            na = s->len[P->leaf_fa];
+            Pa = stage_set(s->ptr[P->leaf_fa], na, 0);
+        }
+        if (P->leaf_fb >= 0) {
+            nb = s->len[P->leaf_fb];
+            Pb = (P->leaf_fb == P->leaf_fa) ? Pa : stage_set(s->ptr[P->leaf_fb], nb, 1);
+        }
+        const int fixA = ka == 0 ? count_outside(s->ptr[sa], s->len[sa], s->chosen, L, lane) : 0;
+        const int fixB = kb == 0 ? count_outside(s->ptr[sb], s->len[sb], s->chosen, L, lane) : 0;
+        const int fixX = (both_fixed && !same)
+                             ? isect_count(s->ptr[sa], s->len[sa], s->ptr[sb], s->len[sb], INT_MAX, s->chosen, L, lane)
+                             : 0;
+        const long long cab = P->leaf_cab, cx = P->leaf_cx;
+        for (int base = 0; base < ncand; base += 32) {
+            const int j = base + lane;
+            bool ok = j < ncand;
+            const int v = ok ? cand[j] : 0;
+            if (ok) ok = !chosen_before(v, L);
+            unsigned st = 0;
+            int len = 0;
+            bool inA = false, inB = false;
+            if (ok) {
+                if (ka == 0) inA = contains(Pa, na, v);
+                if (kb == 0) inB = contains(Pb, nb, v);
+                if (!both_fixed) {
+                    st = g.rowptr[v];
+                    len = (int)(g.rowptr[v + 1] - st);
+                }
+            }
+            s->leafcnt[0][lane] = 0;
+            s->leafcnt[1][lane] = 0;
+            s->leafcnt[2][lane] = 0;
+            __syncwarp();
+            int pre;
+            const int M = warp_scan(len, pre);
+            for (int eb = 0; eb < M; eb += 32) {
+                const int e = eb + lane;
+                const int c = owner(pre, e);
+                const unsigned stc = __shfl_sync(kFull, st, c);
+                const int prc = __shfl_sync(kFull, pre, c);
+                bool ma = false, mb = false;
+                if (e < M) {
+                    const int x = g.col[stc + (e - prc)];
+                    if (!chosen_before(x, L)) {
+                        ma = ka == 1 ? true : contains(Pa, na, x);
+                        mb = kb == 1 ? true : contains(Pb, nb, x);
+                    }
+                }
+                const unsigned grp = __match_any_sync(kFull, e < M ? c : 32 + lane);
+                const unsigned ba = __ballot_sync(kFull, ma), bb = __ballot_sync(kFull, mb),
+                               bx = __ballot_sync(kFull, ma && mb);
+                if (e < M && lane == __ffs(grp) - 1) {
+                    s->leafcnt[0][c] += __popc(ba & grp);
+                    s->leafcnt[1][c] += __popc(bb & grp);
+                    s->leafcnt[2][c] += __popc(bx & grp);
+                }
+                __syncwarp();
+            }
+            if (ok) {
+                const long long A = ka == 0 ? (long long)(fixA - (inA ? 1 : 0)) : s->leafcnt[0][lane];
+                const long long B = kb == 0 ? (long long)(fixB - (inB ? 1 : 0)) : s->leafcnt[1][lane];
+                const long long X = same ? A : (both_fixed ? (long long)(fixX - (inA && inB ? 1 : 0)) : s->leafcnt[2][lane]);
+                total += cab * A * B + cx * X;
+                if (kBytes) bytes += 4ull * (unsigned long long)(len + (ka == 2 ? na : 0) + (kb == 2 ? nb : 0) + A + B) + 8;
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(kFull, total, o);
+        return lane == 0 ? (__int128)total : (__int128)0;
+    }
+
+    // N(v); an id outside the graph is recorded and reads as isolated
+    __device__ __forceinline__ void nbr(int v, const int*& p, int& d) const {
+        if ((unsigned)v >= (unsigned)g.v_cnt) {
+            if (lane == 0) record_check(kErrBadVertex, v, g.v_cnt, P->n, 0, 0, 0);
+            p = g.col;
+            d = 0;
+            return;
+        }
+        const unsigned a = g.rowptr[v], b = g.rowptr[v + 1];
+        p = g.col + a;
+        d = (int)(b - a);
+    }
+
+    __device__ __forceinline__ int bound_of(int d) const {
+        unsigned m = P->rmask[d];
+        int b = g.v_cnt;
+        while (m) {
+            const int j = __ffs(m) - 1;
+            m &= m - 1;
+            b = min(b, s->chosen[j]);
+        }
+        return b;
+    }
+
+    __device__ __forceinline__ bool in_chosen(int v, int d) const {
+        bool hit = false;
+        for (int j = 0; j < d; ++j) hit |= s->chosen[j] == v;
+        return hit;
+    }
+
+    // Lane 0 writes warp-shared state only between two __syncwarp: the first
+    // orders the other lanes' earlier reads before the write (no lane may
+    // see the new value early), the second publishes it.
+    __device__ __forceinline__ void set_chosen(int d, int v) {
+        __syncwarp();
+        if (lane == 0) s->chosen[d] = v;
+        __syncwarp();
+    }
+
+    // Builds the prefix sets whose last member is depth d for candidate v.
+    __device__ bool build_chain(int d, const int* nv, int dv) {
+        const int b = P->chain_begin[d], e = P->chain_begin[d + 1];
+        for (int c = b; c < e; ++c) {
+            const int pid = P->chain_list[c];
+            const int f = P->father[pid];
+            const int* ptr;
+            int len;
+            if (f < 0) {
+                ptr = nv;
+                len = dv;
+            } else {
+                int* dst = scratch + (size_t)P->slot[pid] * cap;
+                const int lf = s->len[f];
+                if (min(lf, dv) > cap) {  // an intersection larger than its slot
+                    if (lane == 0) record_check(kErrSetSize, pid, lf, dv, cap, 0, 0);
+                    return false;
+                }
+                len = isect_store(s->ptr[f], lf, nv, dv, dst, lane);
+                ptr = dst;
+                if (kBytes) bytes += 4ull * (unsigned long long)(lf + dv);
+            }
+            if (lane == 0) {
+                s->ptr[pid] = ptr;
+                s->len[pid] = len;
+            }
+            __syncwarp();
+            if (len == 0) return false;
+        }
+        return true;
+    }
+
+    // inclusion–exclusion tail at depth T (src/graph.cpp:306-344)
+    __device__ __int128 iep_tail() {
+        const int T = P->T, k = P->k;
+        for (int i = 0; i < k; ++i) {
+            const int sid = P->loop_set[T + i];
+            const int v = count_outside(s->ptr[sid], s->len[sid], s->chosen, T, lane);
+            if (v == 0) return 0;  // every group holds a block inside S_i
+            if (lane == 0) s->blockval[i] = v;
+        }
+        const int tmp0 = P->nslots - 2;
+        for (int b = k; b < P->nblocks; ++b) {
+            unsigned m = P->block_mask[b];
+            int j = __ffs(m) - 1;
+            m &= m - 1;
+            const int* A = s->ptr[P->loop_set[T + j]];
+            int na = s->len[P->loop_set[T + j]];
+            int flip = 0;
+            while (__popc(m) > 1 && na > 0) {
+                j = __ffs(m) - 1;
+                m &= m - 1;
+                const int sid = P->loop_set[T + j];
+                int* dst = scratch + (size_t)(tmp0 + flip) * cap;
+                if (kBytes) bytes += 4ull * (unsigned long long)(na + s->len[sid]);
+                na = isect_store(A, na, s->ptr[sid], s->len[sid], dst, lane);
+                A = dst;
+                flip ^= 1;
+            }
+            int val = 0;
+            if (na > 0) {
+                j = __ffs(m) - 1;
+                const int sid = P->loop_set[T + j];
+                if (kBytes) bytes += 4ull * (unsigned long long)(na + s->len[sid]);
+                val = isect_count(A, na, s->ptr[sid], s->len[sid], INT_MAX, s->chosen, T, lane);
+            }
+            if (lane == 0) s->blockval[b] = val;
+        }
+        __syncwarp();
+        __int128 total = 0;
+        if (lane == 0) {
+            for (int g2 = 0; g2 < P->ngroups; ++g2) {
+                __int128 v = P->group_coef[g2];
+                for (int q = P->group_begin[g2]; q < P->group_begin[g2 + 1]; ++q) {
+                    v *= (__int128)s->blockval[P->group_block[q]];
+                    if (v == 0) break;
+                }
+                total += v;
+            }
+        }
+        return total;
+    }
+
+    // the reference's work at depth T once chosen[0, T) and all sets exist
+    __device__ __int128 tail_at_T() {
+        const int T = P->T;
+        const int sid = P->loop_set[T];
+        const int len = s->len[sid];
+        if (len <= 0) return 0;
+        if (P->k) return iep_tail();
+        const int* S = s->ptr[sid];
+        const int lb = lower_bound_u(S, len, bound_of(T));
+        return (__int128)count_outside(S, lb, s->chosen, T, lane);
+    }
+
+    // candidate v at the deepest loop level L
+    __device__ __int128 tail_with_candidate(int v, const int* nv, int dv) {
+        const int L = P->L;
+        if (P->count_only >= 0) {
+            set_chosen(L, v);
+            const int f = P->father[P->count_only];
+            if (kBytes) bytes += 4ull * (unsigned long long)(s->len[f] + dv);
+            return (__int128)isect_count(s->ptr[f], s->len[f], nv, dv, bound_of(P->T), s->chosen, P->T, lane);
+        }
+        if (!build_chain(L, nv, dv)) return 0;
+        set_chosen(L, v);
+        return tail_at_T();
+    }
+
+    __device__ void start_level(int d) {
+        const int sid = P->loop_set[d];
+        const int* S = s->ptr[sid];
+        const int e = lower_bound_u(S, s->len[sid], bound_of(d));
+        __syncwarp();
+        if (lane == 0) {
+            s->lp[d] = S;
+            s->idx[d] = 0;
+            s->end[d] = e;
+            s->dslot[d] = -1;
+        }
+        __syncwarp();
+    }
+
+    // Publishes the loop of depth d (just started) when it is long enough
+    // and a slot is free; the owner's own range then comes from claims.
+    __device__ void maybe_donate(int d) {
+        if (!don || split_min <= 0) return;
+        const int e = s->end[d];
+        if (e < split_min || e > 0xffffff) return;
+        __syncwarp();
+        if (lane == 0) {
+            int h = -1;
+            for (int probe = 0; probe < 4 && h < 0; ++probe) {
+                const int c = (int)((gw * 7 + d * 131 + probe * 257) & (kDonSlots - 1));
+                if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
+            }
+            if (h >= 0) {
+                Donation* r = &don->rec[h];
+                volatile Donation* vr = r;
+                const unsigned gen = ((unsigned)(vr->word >> 48) + 1u) & 0xffffu;
+                vr->pair = pair_idx;
+                vr->depth = d;
+                for (int j = 0; j < d; ++j) vr->chosen[j] = s->chosen[j];
+                __threadfence();
+                atomicExch(&r->word, don_pack(gen, (unsigned)e, 0u));
+                s->dslot[d] = h;
+                s->dgen[d] = gen;
+                s->downer[d] = 1;
+                s->end[d] = 0;
+            }
+        }
+        __syncwarp();
+    }
+
+    // next slice of the donated loop at depth d into idx[d], end[d]
+    __device__ bool claim_more(int d) {
+        int lo = 0, hi = 0;
+        __syncwarp();
+        if ((unsigned)s->dslot[d] >= (unsigned)kDonSlots) {
+            if (lane == 0) record_check(kErrDonation, d, s->dslot[d], 0, 0, 0, 1);
+            return false;
+        }
+        if (lane == 0) {
+            don_claim(&don->rec[s->dslot[d]], s->dgen[d], lo, hi);
+            if (hi > lo) {
+                s->idx[d] = lo;
+                s->end[d] = hi;
+            }
+        }
+        hi = __shfl_sync(kFull, hi, 0);
+        lo = __shfl_sync(kFull, lo, 0);
+        __syncwarp();
+        return hi > lo;
+    }
+
+    // the donated loop at depth d is exhausted: its owner frees the slot
+    __device__ void release(int d) {
+        __syncwarp();
+        if (lane == 0) {
+            if (s->downer[d] && (unsigned)s->dslot[d] < (unsigned)kDonSlots) {
+                __threadfence();
+                atomicExch(&don->busy[s->dslot[d]], 0u);
+            }
+            s->dslot[d] = -1;
+        }
+        __syncwarp();
+    }
+
+    __device__ __forceinline__ bool batch_on() const { return leaf_on && P->leaf_kind != kLeafGeneric; }
+    // pair-sum table keys are 24-bit ids
+    __device__ __forceinline__ bool pair_ready() const { return pair_on && P->pair_ok && g.v_cnt <= (1 << 24); }
+
+    // Loops of depths d0..L; chosen[0, d0), their prefix sets and the loop
+    // range of depth d0 are set.  Returns when depth d0's range (and, for a
+    // donated loop, every slice of it) is done.
+    __device__ __int128 dfs_levels(int d0) {
+        const int L = P->L;
+        const bool batch = batch_on();
+        const bool pair = pair_ready();
+        __int128 acc = 0;
+        int d = d0;
+        while (d >= d0) {
+            const int i = s->idx[d];
+            if (i >= s->end[d]) {
+                if (s->dslot[d] >= 0) {
+                    if (claim_more(d)) continue;
+                    release(d);
+                }
+                --d;
+                continue;
+            }
+            if (i >= s->len[P->loop_set[d]]) {  // a loop range beyond its set
+                if (lane == 0) record_check(kErrLoopIndex, d, i, s->end[d], s->len[P->loop_set[d]], s->dslot[d], 0);
+                --d;
+                continue;
+            }
+            const int v = s->lp[d][i];
+            __syncwarp();
+            if (lane == 0) s->idx[d] = i + 1;
+            __syncwarp();
+            if (in_chosen(v, d)) continue;
+            const int* nv;
+            int dv;
+            nbr(v, nv, dv);
+            if (kBytes) bytes += 8;
+            if (d == L) {
+                acc += tail_with_candidate(v, nv, dv);
+                continue;
+            }
+            if (!build_chain(d, nv, dv)) continue;
+            set_chosen(d, v);
+            ++d;
+            start_level(d);
+            if (batch && d == L) {
+                acc += leaf_batch();
+                --d;
+                continue;
+            }
+            if (pair && d == L - 1) {
+                __int128 r;
+                if (pair_level(r)) {
+                    acc += r;
+                    --d;
+                    continue;
+                }
+            }
+            maybe_donate(d);
+        }
+        return acc;
+    }
+
+    // levels 2..L below a fixed (v0, v1)
+    __device__ __int128 dfs_from_2() {
+        const int L = P->L;
+        start_level(2);
+        if (batch_on() && L == 2) return leaf_batch();
+        if (pair_ready() && L == 3) {
+            __int128 r;
+            if (pair_level(r)) return r;
+        }
+        maybe_donate(2);
+        return dfs_levels(2);
+    }
+
+    // Takes slices of record h (generation gen) until it is exhausted;
+    // false when nothing could be taken.
+    __device__ bool help_one(const PairDesc* pairs, int npairs, unsigned long long* out, int h, unsigned gen) {
+        Donation* r = &don->rec[h];
+        int lo = 0, hi = 0, p = 0, d = 0, rend = 0;
+        if (lane == 0) {
+            const unsigned long long w = *(volatile unsigned long long*)&r->word;
+            if ((unsigned)(w >> 48) == gen && (w & 0xffffffu) < ((w >> 24) & 0xffffffu)) {
+                __threadfence();
+                const volatile Donation* vr = r;
+                p = vr->pair;
+                d = vr->depth;
+                for (int j = 0; j < kMaxN; ++j) s->chosen[j] = j < d ? vr->chosen[j] : -1;
+                rend = (int)((w >> 24) & 0xffffffu);
+                // the claim succeeds only while the record still holds these fields
+                don_claim(r, gen, lo, hi);
+            }
+        }
+        lo = __shfl_sync(kFull, lo, 0);
+        hi = __shfl_sync(kFull, hi, 0);
+        p = __shfl_sync(kFull, p, 0);
+        d = __shfl_sync(kFull, d, 0);
+        rend = __shfl_sync(kFull, rend, 0);
+        __syncwarp();
+        if (hi <= lo) return false;
+        if (p < 0 || p >= npairs) {
+            if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
+            __syncwarp();
+            return true;
+        }
+        const PairDesc pd = pairs[p];
+        P = pd.plan;
+        g = pd.g;
+        cap = pd.cap;
+        pair_idx = p;
+        bool ok = d >= 2 && d <= P->L;
+        for (int l = 0; l < d && ok; ++l) {
+            const int* nv;
+            int dv;
+            nbr(s->chosen[l], nv, dv);
+            ok = build_chain(l, nv, dv);
+        }
+        if (ok) {
+            start_level(d);
+            ok = s->end[d] == rend;
+        }
+        if (!ok) {
+            // the rebuilt loop differs from the published one: the slice is lost
+            if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
+            __syncwarp();
+            return true;
+        }
+        __syncwarp();  // every lane has read end[d] above
+        if (lane == 0) {
+            s->idx[d] = lo;
+            s->end[d] = hi;
+            s->dslot[d] = h;
+            s->dgen[d] = gen;
+            s->downer[d] = 0;
+        }
+        __syncwarp();
+        const __int128 acc = dfs_levels(d);
+        if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
+        return true;
+    }
+
+    // After the warp's own queues: helps published loops until every warp
+    // is done, or no record has had slices left for kIdleRounds scans in a
+    // row (so helpers never hold SMs that blocks not yet resident need).
+    __device__ void help_all(const PairDesc* pairs, int npairs, unsigned long long* out, unsigned total_warps) {
+        constexpr unsigned kIdleRounds = 4096;
+        unsigned idle = 0;
+        for (unsigned round = 0; round < (1u << 24) && idle < kIdleRounds; ++round) {
+            bool worked = false;
+            for (int base = 0; base < kDonSlots; base += 32) {
+                const int h = (int)((gw * 37 + base + lane) & (kDonSlots - 1));
+                const unsigned long long w = *(volatile unsigned long long*)&don->rec[h].word;
+                const bool live = (w & 0xffffffu) < ((w >> 24) & 0xffffffu);
+                unsigned m = __ballot_sync(kFull, live);
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int hj = __shfl_sync(kFull, h, j);
+                    const unsigned long long wj = __shfl_sync(kFull, w, j);
+                    if (help_one(pairs, npairs, out, hj, (unsigned)(wj >> 48))) worked = true;
+                }
+            }
+            if (worked) {
+                idle = 0;
+                continue;
+            }
+            // one lane reads the counter: the exit must be warp-uniform
+            unsigned fin = 0;
+            if (lane == 0) fin = *(volatile unsigned*)&don->finished;
+            if (__shfl_sync(kFull, fin, 0) >= total_warps) return;
+            ++idle;
+            __nanosleep(4000);
+        }
+    }
+
+    __device__ __int128 edge_task(int v0, int v1) {
+        if ((P->rmask[1] & 1u) && v1 >= v0) return 0;
+        const int* n0;
+        int d0;
+        nbr(v0, n0, d0);
+        set_chosen(0, v0);
+        if (!build_chain(0, n0, d0)) return 0;
+        const int* n1;
+        int d1;
+        nbr(v1, n1, d1);
+        if (kBytes) bytes += 16;
+        if (P->L == 1) return tail_with_candidate(v1, n1, d1);
+        if (!build_chain(1, n1, d1)) return 0;
+        set_chosen(1, v1);
+        return dfs_from_2();
+    }
+
+    __device__ __int128 root_task(int v0) {
+        const int* n0;
+        int d0;
+        nbr(v0, n0, d0);
+        if (kBytes) bytes += 8;
+        set_chosen(0, v0);
+        if (!build_chain(0, n0, d0)) return 0;
+        return tail_at_T();
+    }
+};
+
+template <bool kBytes>
+__global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
+                                                    unsigned long long* __restrict__ cursors,
+                                                    unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
+                                                    long long scratch_per_warp, int chunk,
+                                                    const unsigned long long* __restrict__ params,
+                                                    int leaf_on, int stage_cap, int pair_on,
+                                                    unsigned long long* __restrict__ pair_tables, int pair_log2,
+                                                    DonationArea* don, int split_min,
+                                                    unsigned long long* __restrict__ stats) {
+    // params[0] = stripes, params[1] = stripe (device memory, so a captured
+    // graph can replay with new values)
+    const unsigned long long stripes = params[0], stripe = params[1];
+#ifdef GPM_EMU
+    unsigned char* smem_raw = gpm_emu::block_shared();
+#else
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+#endif
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const long long gw = (long long)blockIdx.x * nwarps + wid;
+    WarpCtx<kBytes> w;
+    w.s = reinterpret_cast<WarpState*>(smem_raw) + wid;
+    w.stage = reinterpret_cast<int*>(reinterpret_cast<WarpState*>(smem_raw) + nwarps) + (size_t)wid * 2 * stage_cap;
+    w.stage_cap = stage_cap;
+    w.leaf_on = leaf_on;
+    w.pair_on = pair_on && pair_tables != nullptr;
+    w.pmask = (1u << pair_log2) - 1u;
+    w.ptab = pair_tables ? pair_tables + ((size_t)gw << pair_log2) : nullptr;
+    if (lane == 0) w.s->epoch = 0;  // the first pair sum clears the table
+    w.scratch = scratch_all + gw * scratch_per_warp;
+    w.lane = lane;
+    w.bytes = 0;
+    w.don = don;
+    w.split_min = split_min;
+    w.gw = gw;
+    for (int p = 0; p < npairs; ++p) {
+        const PairDesc pd = pairs[p];
+        w.P = pd.plan;
+        w.g = pd.g;
+        w.cap = pd.cap;
+        w.pair_idx = p;
+        const int T = w.P->T;
+        __int128 acc = 0;
+        int cur_v0 = -1;
+        unsigned cur_lo = 0, cur_hi = 0;
+        for (;;) {
+            // Stripe `stripe` holds the tasks t with t mod stripes == stripe;
+            // grab q takes its members i in [q*chunk, q*chunk + chunk), i.e.
+            // tasks i*stripes + stripe (so the stripe does not depend on chunk).
+            unsigned long long q = 0;
+            if (lane == 0) q = atomicAdd(&cursors[p], 1ull);
+            q = __shfl_sync(kFull, q, 0);
+            const unsigned long long i0 = q * (unsigned long long)chunk;
+            if (i0 * stripes + stripe >= pd.ntasks) break;
+            for (unsigned long long i = i0; i < i0 + (unsigned long long)chunk; ++i) {
+                const unsigned long long t = i * stripes + stripe;
+                if (t >= pd.ntasks) break;
+                if (T == 1) {
+                    acc += w.root_task((int)t);
+                    continue;
+                }
+                const unsigned e = (unsigned)t;
+                if (cur_v0 < 0 || e < cur_lo || e >= cur_hi) {
+                    // last v with rowptr[v] <= e
+                    int lo = 0, hi = pd.g.v_cnt;
+                    while (lo < hi) {
+                        int mid = (lo + hi + 1) >> 1;
+                        if (pd.g.rowptr[mid] <= e) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    cur_v0 = lo;
+                    cur_lo = pd.g.rowptr[lo];
+                    cur_hi = pd.g.rowptr[lo + 1];
+                }
+                acc += w.edge_task(cur_v0, pd.g.col[e]);
+            }
+        }
+        if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
+    }
+    if (don) {
+        if (lane == 0) {
+            __threadfence();
+            atomicAdd(&don->finished, 1u);
+        }
+        __syncwarp();
+        w.help_all(pairs, npairs, out, gridDim.x * (unsigned)nwarps);
+    }
+    if (kBytes && lane == 0 && w.bytes) atomicAdd(stats, w.bytes);
+}
