@@ -4,9 +4,9 @@ a/b/c/d = .57/.19/.19/.05, seed 3), one persistent launch per step.
 
 A step is one launch over one stripe of the first-level work: the
 schedule-driven enumeration of all 29 motifs for the first-level tasks
-(root, first neighbour) in work chunks q*S + s of the stripe s, S stripes in
-all (the same interleaved partition that splits the job across GPUs).
-Successive steps take successive stripes; S steps cover the whole job.
+(root, first neighbour) t with t mod S = s, S stripes in all (the same
+interleaved partition that splits the job across GPUs).  Successive steps
+take successive stripes; S steps cover the whole job.
 The graph (0.5 GB of CSR, larger than the 129 MB L2) stays resident in HBM.
 
 Reported on one JSON line (rank 0):
@@ -134,6 +134,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     gh = (C.c_void_p * n)(*([g.device()] * n))
     ph = (C.c_void_p * n)(*[p.handle for p in plans])
     gp.set_option("raw_sums", 1)
+    gp.set_option("pair_log2", args.pair_log2)
 
     def batched(stripe: int) -> list[int]:
         gp.set_option("stripe", stripe)
@@ -149,18 +150,22 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         return (i * world + rank) % S
 
     if args.stripes == "auto":
-        # calibrate: time one launch over a thin stripe, then size a step to
-        # about --step-seconds of kernel time (power of two, 1..2^22)
-        S0 = 1 << 20
-        gp.set_option("stripes", S0)
-        batched(S0 - 1)
-        t0 = max(gp.last_launch_stats()[0], 1e-3)
+        # calibrate from the thinnest stripe (about one task per motif):
+        # double the work until a launch takes a quarter of --step-seconds,
+        # then extrapolate to a step of about --step-seconds (power of two)
         want = args.step_seconds * 1e3
-        S = S0
-        while S > 1 and t0 * S0 / S * 2 <= want:
+        S = 1 << 27
+        while True:
+            gp.set_option("stripes", S)
+            batched(S - 1)
+            t = max(gp.last_launch_stats()[0], 1e-3)
+            print(f"[bench] calibrate: stripes={S} {t:.1f} ms", file=sys.stderr, flush=True)
+            if t >= want / 4 or S == 1:
+                break
             S //= 2
-        while S < (1 << 22) and t0 * S0 / S > want * 2:
-            S *= 2
+        while S > 1 and t * 2 <= want:
+            S //= 2
+            t *= 2
     else:
         S = int(args.stripes)
     gp.set_option("stripes", S)
@@ -195,14 +200,16 @@ def run_ours(args, rank: int, world: int) -> dict | None:
 
     print(f"[bench] timed: {elapsed_ms:.1f} ms for {args.steps} steps", file=sys.stderr, flush=True)
     # ---- plain: one launch per pattern over the same stripes -------------
-    plain_ms = []
+    plain_ms, by_motif = [], [[] for _ in plans]
     for i in range(args.steps):
         gp.set_option("stripe", stripe_of(i))
         tot = 0.0
         for j, p in enumerate(plans):
             o = native.U128()
             native.check(gp.lib().gpm_count(g.device(), p.handle, C.byref(o)), "gpm_count")
-            tot += gp.last_launch_stats()[0]
+            ms = gp.last_launch_stats()[0]
+            tot += ms
+            by_motif[j].append(ms)
             if _signed(o.value) != raws_all[i][j]:
                 raise AssertionError(f"plain and batched counts differ for motif {j}")
         plain_ms.append(tot)
@@ -269,6 +276,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         },
         "kernel_ms_per_step": statistics.median(kernel_ms),
         "plain_per_pattern_ms_per_step": statistics.median(plain_ms),
+        "plain_ms_by_motif": [round(sum(m), 2) for m in by_motif],
         "batched_speedup_vs_plain": statistics.median(plain_ms) / statistics.median(kernel_ms),
         "embeddings_per_step": emb / args.steps,
         "e2e": {"value": e2e_emb / (e2e_ms / 1e3), "unit": "embeddings/s",
@@ -354,6 +362,8 @@ def main() -> None:
     ap.add_argument("--step-seconds", type=float, default=4.0)
     ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark graph)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--pair-log2", type=int, default=0,
+                    help="entries per warp of the pair-sum table as a power of two (0: sized to free memory)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))

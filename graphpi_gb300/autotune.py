@@ -14,6 +14,7 @@ Knobs (gpm_set_option):
   blocks_per_sm             persistent blocks per SM
   stage_max                 largest fixed set staged in shared memory (ints)
   leaf_batch                batched deepest loop level on/off
+  pair_leaf                 pair sums over the last two loops on/off
   split                     shortest loop (depth >= 2) shared with idle warps
   merge_alpha4_{small,mid,large}
                             merge vs binary-search weight for lists shorter
@@ -37,6 +38,7 @@ SPACE = {
     "blocks_per_sm": [1, 2, 3],
     "stage_max": [0, 256, 1024, 2048],
     "leaf_batch": [0, 1],
+    "pair_leaf": [0, 1],
     "split": [0, 16, 64, 256],
     "merge_alpha4_small": [0, 2, 4, 8, 32],
     "merge_alpha4_mid": [0, 2, 4, 8, 32],

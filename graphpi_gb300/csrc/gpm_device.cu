@@ -344,6 +344,10 @@ static GraphView view_of(const gpm_graph* g, bool caller_ids = false) {
     return v;
 }
 
+// Pair-sum tables: 2^pair_log2 64-bit words per warp, at most a quarter of
+// the free memory left after the set slots (2^13 .. 2^20 words unless forced).
+constexpr int kPairLog2Min = 13, kPairLog2Max = 20;
+
 struct LaunchSetup {
     std::vector<PairDesc> descs;
     long long blocks = 0;
@@ -354,11 +358,11 @@ struct LaunchSetup {
     int chunk = 0;
     int leaf_on = 0;
     int pair_on = 0;
+    int pair_log2 = kPairLog2Min;
     int split_min = 0;
     bool count_bytes = false;
 };
 
-constexpr int kPairLog2 = 13;  // 8192-entry table per warp
 
 // Validates the pairs and sizes the launch from the current options.
 static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_plan* const* plans,
@@ -419,6 +423,17 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         for (int i = 0; i < n; ++i) any |= plans[i]->host.pair_ok && graphs[i]->v_cnt <= (1 << 24);
         ls.pair_on = any ? 1 : 0;
     }
+    if (ls.pair_on) {
+        const size_t warps = (size_t)ls.blocks * ls.wpb;
+        const size_t sets = warps * (size_t)ls.per_warp * sizeof(int);
+        const size_t room = (free_b + scratch_budget_extra) > sets ? (free_b + scratch_budget_extra - sets) / 4 : 0;
+        if (o.pair_log2) {
+            ls.pair_log2 = (int)o.pair_log2;
+        } else {
+            ls.pair_log2 = kPairLog2Max;
+            while (ls.pair_log2 > kPairLog2Min && warps * ((size_t)8 << ls.pair_log2) > room) --ls.pair_log2;
+        }
+    }
     ls.split_min = (int)o.split;
     return GPM_OK;
 }
@@ -438,7 +453,7 @@ static ScratchLayout scratch_layout(const LaunchSetup& ls) {
     size_t b = warps * (size_t)ls.per_warp * sizeof(int);
     b = (b + 255) & ~(size_t)255;
     s.tables = b;
-    if (ls.pair_on) b += warps * ((size_t)1 << kPairLog2) * sizeof(unsigned long long);
+    if (ls.pair_on) b += warps * ((size_t)1 << ls.pair_log2) * sizeof(unsigned long long);
     s.donation = b;
     if (ls.split_min > 0) b += sizeof(DonationArea);
     s.total = std::max<size_t>(b, 1);
@@ -463,11 +478,11 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
     if (ls.count_bytes)
         match_kernel<true><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
             d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
-            tables, kPairLog2, don, ls.split_min, stats);
+            tables, ls.pair_log2, don, ls.split_min, stats);
     else
         match_kernel<false><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
             d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
-            tables, kPairLog2, don, ls.split_min, stats);
+            tables, ls.pair_log2, don, ls.split_min, stats);
     return cudaGetLastError();
 }
 

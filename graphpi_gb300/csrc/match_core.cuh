@@ -388,8 +388,8 @@ struct WarpCtx {
     // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
     // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
     // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
-    // (and does nothing) when B's neighbour lists would fill the table more
-    // than half: the caller then runs the level normally.
+    // (and does nothing) when the smaller side's neighbour lists would fill
+    // the table more than half: the caller then runs the level normally.
     __device__ bool pair_level(__int128& out) {
         const int L1 = P->L - 1;
         const int T = P->T;
@@ -399,22 +399,32 @@ struct WarpCtx {
         const int* candB = s->ptr[sb];
         const int nb = lower_bound_u(candB, s->len[sb], bound_of(P->L));
         const int bnd = bound_of(T);
-        // size of B's neighbour lists below the bound
-        long long mb = 0;
-        for (int base = 0; base < nb; base += 32) {
-            const int j = base + lane;
-            int len = 0;
-            if (j < nb) {
-                const int w = candB[j];
-                if (!chosen_before(w, L1)) {
-                    const unsigned st = g.rowptr[w];
-                    len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
+        // sizes of A's and B's neighbour lists below the bound; the smaller
+        // side fills the table, the other probes it (the sum is symmetric)
+        long long ma = 0, mb = 0;
+        for (int side = 0; side < 2; ++side) {
+            const int* cand = side == 0 ? candA : candB;
+            const int nc = side == 0 ? na : nb;
+            long long m = 0;
+            for (int base = 0; base < nc; base += 32) {
+                const int j = base + lane;
+                int len = 0;
+                if (j < nc) {
+                    const int w = cand[j];
+                    if (!chosen_before(w, L1)) {
+                        const unsigned st = g.rowptr[w];
+                        len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
+                    }
                 }
+                int pre;
+                m += warp_scan(len, pre);
             }
-            int pre;
-            mb += warp_scan(len, pre);
+            (side == 0 ? ma : mb) = m;
         }
-        if (mb * 2 > (long long)pmask + 1) return false;
+        const long long mins = min(ma, mb);
+        if (mins * 2 > (long long)pmask + 1) return false;
+        const bool a_fills = ma < mb;
+        __syncwarp();
         if (lane == 0) {
             s->epoch = (s->epoch + 1) & 0xffffu;
             if (s->epoch == 0) s->epoch = 1;
@@ -426,10 +436,11 @@ struct WarpCtx {
             __syncwarp();
         }
         long long sum = 0;
-        // phase 1 (B -> counts) and phase 2 (A -> sum of counts)
+        // phase 0 (smaller side -> counts) and phase 1 (other side -> sum of counts)
         for (int phase = 0; phase < 2; ++phase) {
-            const int* cand = phase == 0 ? candB : candA;
-            const int nc = phase == 0 ? nb : na;
+            const bool use_a = (phase == 0) == a_fills;
+            const int* cand = use_a ? candA : candB;
+            const int nc = use_a ? na : nb;
             for (int base = 0; base < nc; base += 32) {
                 const int j = base + lane;
                 unsigned st = 0;
@@ -453,7 +464,7 @@ struct WarpCtx {
                         const int x = g.col[stc + (e - prc)];
                         if (!chosen_before(x, L1)) {
                             if (phase == 0) {
-                                if (!pair_add(ptab, pmask, ep, x)) record_check(3, x, mb, pmask, 0, 0, 0);
+                                if (!pair_add(ptab, pmask, ep, x)) record_check(3, x, mins, pmask, 0, 0, 0);
                             } else {
                                 sum += pair_get(ptab, pmask, ep, x);
                             }

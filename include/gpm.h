@@ -240,7 +240,9 @@ GPM_API int gpm_mlp_train(gpm_mlp* m, const float* X, const float* T, int32_t n_
  *   "split" (a loop at depth >= 2 with at least this many candidates is
  *   published so that idle warps take slices of it; 0 = off),
  *   "stage_max" (largest father set staged in shared memory),
- *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan allows),
+ *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan allows;
+ *   both on by default), "pair_log2" (entries per warp of the pair-sum
+ *   table as a power of two; 0 = sized to free memory),
  *   "merge_alpha4_small"/"_mid"/"_large" (merge vs search per length bucket),
  *   "timeout_ms" (bounded waits),
  *   "stripes"/"stripe" (a launch covers only the first-level tasks t with

@@ -108,7 +108,7 @@ std::vector<Sched> motif_schedules(const Csr& g, int k, bool iep, int stride) {
 }
 
 struct Knobs {
-    int blocks = 2, wpb = 4, chunk = 2, stage_cap = 64, leaf = 1, pair = 0, split = 0;
+    int blocks = 2, wpb = 4, chunk = 2, stage_cap = 64, leaf = 1, pair = 0, split = 0, pair_log2 = 13;
     unsigned long long stripes = 1, stripe = 0;
 };
 
@@ -141,7 +141,7 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     std::vector<unsigned long long> cursors(n, 0), out(2 * n, 0), stats(2, 0);
     unsigned long long params[2] = {k.stripes, k.stripe};
     std::vector<unsigned long long> tables;
-    if (k.pair) tables.assign((size_t)warps << 13, 0ull);
+    if (k.pair) tables.assign((size_t)warps << k.pair_log2, 0ull);
     DonationArea* don = k.split > 0 ? new DonationArea() : nullptr;
     if (don) std::memset((void*)don, 0, sizeof(DonationArea));
     const size_t smem = sizeof(WarpState) * k.wpb + sizeof(int) * 2 * (size_t)k.stage_cap * k.wpb;
@@ -161,7 +161,7 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
                 }
                 auto body = [&](int) {
                     match_kernel<false>(pairs.data(), n, cursors.data(), out.data(), scratch.data(), per_warp, k.chunk,
-                                        params, k.leaf, k.stage_cap, k.pair, k.pair ? tables.data() : nullptr, 13, don,
+                                        params, k.leaf, k.stage_cap, k.pair, k.pair ? tables.data() : nullptr, k.pair_log2, don,
                                         k.split, stats.data());
                 };
                 gpm_emu::run_warp(*w, body);
@@ -261,12 +261,14 @@ void case_pair() {
         ++failures;
         return;
     }
-    for (int split : {0, 1}) {
-        Knobs k;
-        k.pair = 1;
-        k.split = split;
-        expect_oracle("pair-sum", g, ss, k);
-    }
+    for (int split : {0, 1})
+        for (int log2 : {13, 5}) {  // a table that holds every task, and one that forces the fallback
+            Knobs k;
+            k.pair = 1;
+            k.split = split;
+            k.pair_log2 = log2;
+            expect_oracle("pair-sum", g, ss, k);
+        }
 }
 
 void case_stripes() {

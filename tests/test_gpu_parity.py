@@ -302,8 +302,11 @@ def test_pair_sum_leaf_matches_oracle(engine, oracle):
         assert scheds, "no plan takes the pair-sum leaf"
         want = [oracle.count(g, s) for s in scheds]
         for split in (0, 1):
-            got = _with_options({"pair_leaf": 1, "split": split}, lambda: gp.batch_count([g] * len(scheds), scheds))
-            assert got == want, split
+            for log2 in (0, 6):  # tables sized to memory, and tiny ones that force the fallback
+                opts = {"pair_leaf": 1, "split": split, "pair_log2": log2}
+                got = _with_options(opts, lambda: gp.batch_count([g] * len(scheds), scheds))
+                assert got == want, (split, log2)
+        assert _with_options({"pair_leaf": 0}, lambda: gp.batch_count([g] * len(scheds), scheds)) == want
 
 
 def test_stripes_do_not_depend_on_chunk(engine):
