@@ -15,6 +15,8 @@ Knobs (gpm_set_option):
   stage_max                 largest fixed set staged in shared memory (ints)
   leaf_batch                batched deepest loop level on/off
   pair_leaf                 pair sums over the last two loops on/off
+  bitmap_min                smallest fixed leaf set tested through a bitmap
+                            (the bitmap-vs-search threshold by set size)
   split                     shortest loop (depth >= 2) shared with idle warps
   merge_alpha4_{small,mid,large}
                             merge vs binary-search weight for lists shorter
@@ -39,6 +41,7 @@ SPACE = {
     "stage_max": [0, 256, 1024, 2048],
     "leaf_batch": [0, 1],
     "pair_leaf": [0, 1],
+    "bitmap_min": [0, 1024, 4096, 16384],
     "split": [0, 16, 64, 256],
     "merge_alpha4_small": [0, 2, 4, 8, 32],
     "merge_alpha4_mid": [0, 2, 4, 8, 32],

@@ -686,6 +686,7 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "leaf_batch") slot = &o.leaf_batch, lo = 0, hi = 1;
     else if (k == "pair_leaf") slot = &o.pair_leaf, lo = 0, hi = 1;
     else if (k == "pair_log2") slot = &o.pair_log2, lo = 0, hi = 24;
+    else if (k == "bitmap_min") slot = &o.bitmap_min, lo = 0, hi = 1 << 30;
     else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
     else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;
     else if (k == "stripe") slot = &o.stripe, lo = 0, hi = (1 << 30) - 1;
@@ -719,6 +720,7 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "leaf_batch") *value = o.leaf_batch;
     else if (k == "pair_leaf") *value = o.pair_leaf;
     else if (k == "pair_log2") *value = o.pair_log2;
+    else if (k == "bitmap_min") *value = o.bitmap_min;
     else if (k == "split") *value = o.split;
     else if (k == "stripes") *value = o.stripes;
     else if (k == "stripe") *value = o.stripe;

@@ -360,6 +360,8 @@ struct LaunchSetup {
     int pair_on = 0;
     int pair_log2 = kPairLog2Min;
     int split_min = 0;
+    int bm_words = 0;  // words per leaf bitmap (0: no bitmaps)
+    int bm_min = 0;
     bool count_bytes = false;
 };
 
@@ -435,6 +437,20 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         }
     }
     ls.split_min = (int)o.split;
+    // two bitmaps over vertex ids per warp for the batched leaves
+    ls.bm_words = 0;
+    ls.bm_min = (int)o.bitmap_min;
+    if (ls.leaf_on && ls.bm_min > 0) {
+        int vmax = 0;
+        bool any = false;
+        for (int i = 0; i < n; ++i) {
+            vmax = std::max(vmax, graphs[i]->v_cnt);
+            any |= plans[i]->host.leaf_kind != kLeafGeneric;
+        }
+        const size_t words = ((size_t)vmax + 31) / 32;
+        const size_t warps = (size_t)ls.blocks * ls.wpb;
+        if (any && warps * 2 * words * sizeof(unsigned) <= (free_b + scratch_budget_extra) / 8) ls.bm_words = (int)words;
+    }
     return GPM_OK;
 }
 
@@ -444,8 +460,12 @@ static size_t small_words(int n) { return (size_t)n * 3 + 4; }
 // Scratch of a launch: per-warp set slots, per-warp pair tables, then the
 // donation records (zeroed before every launch).
 struct ScratchLayout {
-    size_t tables = 0, donation = 0, total = 0;
+    size_t tables = 0, donation = 0, bitmaps = 0, total = 0;
 };
+
+static size_t bitmap_bytes(const LaunchSetup& ls) {
+    return (size_t)ls.blocks * ls.wpb * 2 * (size_t)ls.bm_words * sizeof(unsigned);
+}
 
 static ScratchLayout scratch_layout(const LaunchSetup& ls) {
     const size_t warps = (size_t)ls.blocks * ls.wpb;
@@ -456,6 +476,9 @@ static ScratchLayout scratch_layout(const LaunchSetup& ls) {
     if (ls.pair_on) b += warps * ((size_t)1 << ls.pair_log2) * sizeof(unsigned long long);
     s.donation = b;
     if (ls.split_min > 0) b += sizeof(DonationArea);
+    b = (b + 255) & ~(size_t)255;
+    s.bitmaps = b;
+    b += bitmap_bytes(ls);
     s.total = std::max<size_t>(b, 1);
     return s;
 }
@@ -475,14 +498,19 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
         const cudaError_t e = cudaMemsetAsync(don, 0, sizeof(DonationArea), st);
         if (e != cudaSuccess) return e;
     }
+    unsigned* bitmaps = ls.bm_words ? (unsigned*)((char*)scratch + lay.bitmaps) : nullptr;
+    if (bitmaps) {
+        const cudaError_t e = cudaMemsetAsync(bitmaps, 0, bitmap_bytes(ls), st);
+        if (e != cudaSuccess) return e;
+    }
     if (ls.count_bytes)
         match_kernel<true><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
             d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
-            tables, ls.pair_log2, don, ls.split_min, stats);
+            tables, ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, stats);
     else
         match_kernel<false><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
             d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
-            tables, ls.pair_log2, don, ls.split_min, stats);
+            tables, ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, stats);
     return cudaGetLastError();
 }
 

@@ -79,7 +79,8 @@ struct Donation {
     int pair;
     int depth;
     int chosen[kMaxN];
-    int pad_[4];
+    int leaf;  // 1: the batched deepest level, taken in coarser slices
+    int pad_[3];
 };
 static_assert(sizeof(Donation) == 64, "one record per 64 bytes");
 
@@ -96,17 +97,19 @@ __device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned en
 }
 
 // Takes the next slice of record r (generation gen); lo == hi when the loop
-// is exhausted or the slot holds another generation.  Lock-free: a failed
-// compare-and-swap means another warp took a slice, so the retries are
-// bounded by the loop length (< 2^24).
-__device__ void don_claim(Donation* r, unsigned gen, int& lo, int& hi) {
+// is exhausted or the slot holds another generation.  A slice is 1/32 of
+// what is left, within [1, 64] candidates of a loop or [32, 1024] of a
+// batched leaf level.  Lock-free: a failed compare-and-swap means another
+// warp took a slice, so the retries are bounded by the loop length (< 2^24).
+__device__ void don_claim(Donation* r, unsigned gen, bool leaf, int& lo, int& hi) {
     lo = hi = 0;
     unsigned long long w = *(volatile unsigned long long*)&r->word;
     for (int tries = 0; tries < (1 << 25); ++tries) {
         if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
         const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
         if (next >= end) return;
-        const unsigned take = min(64u, max(1u, (end - next) >> 5));
+        const unsigned want = (end - next) >> 5;
+        const unsigned take = min(end - next, leaf ? min(1024u, max(32u, want)) : min(64u, max(1u, want)));
         const unsigned long long got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
         if (got == w) {
             lo = (int)next;
@@ -342,9 +345,35 @@ struct WarpCtx {
     unsigned pmask;
     DonationArea* don;         // null: no donation
     int split_min;             // smallest loop that is donated
+    unsigned* bm;              // this warp's two bitmaps over vertex ids (null: none)
+    int bm_words;              // words per bitmap
+    int bm_min;                // smallest fixed set tested through a bitmap
     int pair_idx;              // pair whose work is running
     long long gw;              // global warp index
     unsigned long long bytes;
+
+    // Bitmap variant of a membership test: marks set S[0, n) in bitmap r.
+    // Used for fixed sets too large for shared memory when the elements to
+    // test outnumber an eighth of the set: one load per test instead of a
+    // binary search of log2(n) dependent loads.  bitmap_clear undoes it.
+    __device__ const unsigned* bitmap_set(const int* S, int n, int r) {
+        unsigned* b = bm + (size_t)r * bm_words;
+        for (int i = lane; i < n; i += 32) {
+            const int x = S[i];
+            atomicOr(&b[x >> 5], 1u << (x & 31));
+        }
+        __syncwarp();
+        return b;
+    }
+    __device__ void bitmap_clear(const int* S, int n, int r) {
+        unsigned* b = bm + (size_t)r * bm_words;
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) b[S[i] >> 5] = 0u;
+        __syncwarp();
+    }
+    __device__ __forceinline__ bool use_bitmap(int n, long long tests) const {
+        return bm != nullptr && bm_min > 0 && n > stage_cap && n >= bm_min && tests * 8 >= n;
+    }
 
     // copies a fixed set into shared-memory region r when it fits
     __device__ const int* stage_set(const int* p, int n, int r) {
@@ -495,12 +524,29 @@ struct WarpCtx {
         return true;
     }
 
-    // All candidates of level L at once (the plan's leaf_kind says how the
-    // tail reads N(v)); chosen[0, L) and the level's loop list are set.
-    __device__ __int128 leaf_batch() {
+    // Σ deg(v) over the candidates not chosen before depth L (warp-uniform)
+    __device__ long long list_total(const int* cand, int ncand, int L) {
+        long long m = 0;
+        for (int base = 0; base < ncand; base += 32) {
+            const int j = base + lane;
+            int len = 0;
+            if (j < ncand) {
+                const int v = cand[j];
+                if (!chosen_before(v, L)) len = (int)(g.rowptr[v + 1] - g.rowptr[v]);
+            }
+            int pre;
+            m += warp_scan(len, pre);
+        }
+        return m;
+    }
+
+    // Candidates [lo, hi) of level L at once (the plan's leaf_kind says how
+    // the tail reads N(v)); chosen[0, L) and the level's loop list are set.
+    // The result is a sum over candidates, so slices add up.
+    __device__ __int128 leaf_batch(int lo, int hi) {
         const int L = P->L, T = P->T;
-        const int* cand = s->lp[L];
-        const int ncand = s->end[L];
+        const int* cand = s->lp[L] + lo;
+        const int ncand = hi - lo;
         long long total = 0;
         if (P->leaf_kind == kLeafCount) {
             // bound of the last loop: restrictions on depths < L are fixed
@@ -510,12 +556,14 @@ struct WarpCtx {
                 if (m >> j & 1) bfix = min(bfix, s->chosen[j]);
             const bool by_v = (m >> L) & 1;
             const int* F = nullptr;
+            const unsigned* FB = nullptr;
             int nf = 0, lim = bfix;
             if (P->leaf_fa >= 0) {
                 nf = lower_bound_u(s->ptr[P->leaf_fa], s->len[P->leaf_fa], bfix);
                 if (nf == 0) return 0;
                 F = stage_set(s->ptr[P->leaf_fa], nf, 0);
                 lim = min(bfix, F[nf - 1] + 1);
+                if (use_bitmap(nf, list_total(cand, ncand, L))) FB = bitmap_set(F, nf, 0);
             }
             for (int base = 0; base < ncand; base += 32) {
                 const int j = base + lane;
@@ -541,11 +589,12 @@ struct WarpCtx {
                     if (e < M) {
                         const int x = g.col[stc + (e - prc)];
                         hit = !chosen_before(x, L);
-                        if (hit && F) hit = contains(F, nf, x);
+                        if (hit && F) hit = FB ? ((FB[x >> 5] >> (x & 31)) & 1u) != 0 : contains(F, nf, x);
                     }
                     total += __popc(__ballot_sync(kFull, hit));
                 }
             }
+            if (FB) bitmap_clear(F, nf, 0);
             return lane == 0 ? (__int128)total : (__int128)0;
         }
         // ---- two-loop inclusion–exclusion tail ----
@@ -562,6 +611,14 @@ struct WarpCtx {
             nb = s->len[P->leaf_fb];
             Pb = (P->leaf_fb == P->leaf_fa) ? Pa : stage_set(s->ptr[P->leaf_fb], nb, 1);
         }
+        const unsigned* BA = nullptr;
+        const unsigned* BB = nullptr;
+        if (bm && ((Pa && na > stage_cap) || (Pb && nb > stage_cap))) {
+            const long long tests = both_fixed ? (long long)ncand : list_total(cand, ncand, L);
+            if (Pa && use_bitmap(na, tests)) BA = bitmap_set(Pa, na, 0);
+            if (Pb && Pb == Pa) BB = BA;
+            else if (Pb && use_bitmap(nb, tests)) BB = bitmap_set(Pb, nb, 1);
+        }
         const int fixA = ka == 0 ? count_outside(s->ptr[sa], s->len[sa], s->chosen, L, lane) : 0;
         const int fixB = kb == 0 ? count_outside(s->ptr[sb], s->len[sb], s->chosen, L, lane) : 0;
         const int fixX = (both_fixed && !same)
@@ -577,8 +634,8 @@ struct WarpCtx {
             int len = 0;
             bool inA = false, inB = false;
             if (ok) {
-                if (ka == 0) inA = contains(Pa, na, v);
-                if (kb == 0) inB = contains(Pb, nb, v);
+                if (ka == 0) inA = BA ? ((BA[v >> 5] >> (v & 31)) & 1u) != 0 : contains(Pa, na, v);
+                if (kb == 0) inB = BB ? ((BB[v >> 5] >> (v & 31)) & 1u) != 0 : contains(Pb, nb, v);
                 if (!both_fixed) {
                     st = g.rowptr[v];
                     len = (int)(g.rowptr[v + 1] - st);
@@ -599,8 +656,8 @@ struct WarpCtx {
                 if (e < M) {
                     const int x = g.col[stc + (e - prc)];
                     if (!chosen_before(x, L)) {
-                        ma = ka == 1 ? true : contains(Pa, na, x);
-                        mb = kb == 1 ? true : contains(Pb, nb, x);
+                        ma = ka == 1 ? true : (BA ? ((BA[x >> 5] >> (x & 31)) & 1u) != 0 : contains(Pa, na, x));
+                        mb = kb == 1 ? true : (BB ? ((BB[x >> 5] >> (x & 31)) & 1u) != 0 : contains(Pb, nb, x));
                     }
                 }
                 const unsigned grp = __match_any_sync(kFull, e < M ? c : 32 + lane);
@@ -622,6 +679,8 @@ struct WarpCtx {
             }
             __syncwarp();
         }
+        if (BA) bitmap_clear(Pa, na, 0);
+        if (BB && BB != BA) bitmap_clear(Pb, nb, 1);
 #pragma unroll
         for (int o = 16; o >= 1; o >>= 1) total += __shfl_xor_sync(kFull, total, o);
         return lane == 0 ? (__int128)total : (__int128)0;
@@ -808,6 +867,7 @@ struct WarpCtx {
                 const unsigned gen = ((unsigned)(vr->word >> 48) + 1u) & 0xffffu;
                 vr->pair = pair_idx;
                 vr->depth = d;
+                vr->leaf = (d == P->L && batch_on()) ? 1 : 0;
                 for (int j = 0; j < d; ++j) vr->chosen[j] = s->chosen[j];
                 __threadfence();
                 atomicExch(&r->word, don_pack(gen, (unsigned)e, 0u));
@@ -829,7 +889,7 @@ struct WarpCtx {
             return false;
         }
         if (lane == 0) {
-            don_claim(&don->rec[s->dslot[d]], s->dgen[d], lo, hi);
+            don_claim(&don->rec[s->dslot[d]], s->dgen[d], d == P->L && batch_on(), lo, hi);
             if (hi > lo) {
                 s->idx[d] = lo;
                 s->end[d] = hi;
@@ -857,6 +917,23 @@ struct WarpCtx {
     __device__ __forceinline__ bool batch_on() const { return leaf_on && P->leaf_kind != kLeafGeneric; }
     // pair-sum table keys are 24-bit ids
     __device__ __forceinline__ bool pair_ready() const { return pair_on && P->pair_ok && g.v_cnt <= (1 << 24); }
+
+    // The batched deepest level: its range [idx, end), then (when the level
+    // is published) every further slice the warp can claim.
+    __device__ __int128 leaf_slices() {
+        const int L = P->L;
+        __int128 acc = 0;
+        for (;;) {
+            const int lo = s->idx[L], hi = s->end[L];
+            if (lo < hi) acc += leaf_batch(lo, hi);
+            if (s->dslot[L] < 0) break;
+            if (!claim_more(L)) {
+                release(L);
+                break;
+            }
+        }
+        return acc;
+    }
 
     // Loops of depths d0..L; chosen[0, d0), their prefix sets and the loop
     // range of depth d0 are set.  Returns when depth d0's range (and, for a
@@ -900,7 +977,8 @@ struct WarpCtx {
             ++d;
             start_level(d);
             if (batch && d == L) {
-                acc += leaf_batch();
+                maybe_donate(L);
+                acc += leaf_slices();
                 --d;
                 continue;
             }
@@ -921,7 +999,10 @@ struct WarpCtx {
     __device__ __int128 dfs_from_2() {
         const int L = P->L;
         start_level(2);
-        if (batch_on() && L == 2) return leaf_batch();
+        if (batch_on() && L == 2) {
+            maybe_donate(2);
+            return leaf_slices();
+        }
         if (pair_ready() && L == 3) {
             __int128 r;
             if (pair_level(r)) return r;
@@ -943,9 +1024,10 @@ struct WarpCtx {
                 p = vr->pair;
                 d = vr->depth;
                 for (int j = 0; j < kMaxN; ++j) s->chosen[j] = j < d ? vr->chosen[j] : -1;
+                const bool leaf = vr->leaf != 0;
                 rend = (int)((w >> 24) & 0xffffffu);
                 // the claim succeeds only while the record still holds these fields
-                don_claim(r, gen, lo, hi);
+                don_claim(r, gen, leaf, lo, hi);
             }
         }
         lo = __shfl_sync(kFull, lo, 0);
@@ -991,7 +1073,7 @@ struct WarpCtx {
             s->downer[d] = 0;
         }
         __syncwarp();
-        const __int128 acc = dfs_levels(d);
+        const __int128 acc = (d == P->L && batch_on()) ? leaf_slices() : dfs_levels(d);
         if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
         return true;
     }
@@ -1066,7 +1148,8 @@ __global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restric
                                                     const unsigned long long* __restrict__ params,
                                                     int leaf_on, int stage_cap, int pair_on,
                                                     unsigned long long* __restrict__ pair_tables, int pair_log2,
-                                                    DonationArea* don, int split_min,
+                                                    DonationArea* don, int split_min, unsigned* bitmaps,
+                                                    int bm_words, int bm_min,
                                                     unsigned long long* __restrict__ stats) {
     // params[0] = stripes, params[1] = stripe (device memory, so a captured
     // graph can replay with new values)
@@ -1094,6 +1177,9 @@ __global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restric
     w.don = don;
     w.split_min = split_min;
     w.gw = gw;
+    w.bm = bitmaps ? bitmaps + (size_t)gw * 2 * (size_t)bm_words : nullptr;
+    w.bm_words = bm_words;
+    w.bm_min = bm_min;
     for (int p = 0; p < npairs; ++p) {
         const PairDesc pd = pairs[p];
         w.P = pd.plan;

@@ -242,7 +242,9 @@ GPM_API int gpm_mlp_train(gpm_mlp* m, const float* X, const float* T, int32_t n_
  *   "stage_max" (largest father set staged in shared memory),
  *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan allows;
  *   both on by default), "pair_log2" (entries per warp of the pair-sum
- *   table as a power of two; 0 = sized to free memory),
+ *   table as a power of two; 0 = sized to free memory), "bitmap_min"
+ *   (fixed leaf sets at least this large are tested through a per-warp
+ *   bitmap instead of a binary search; 0 = never),
  *   "merge_alpha4_small"/"_mid"/"_large" (merge vs search per length bucket),
  *   "timeout_ms" (bounded waits),
  *   "stripes"/"stripe" (a launch covers only the first-level tasks t with

@@ -39,6 +39,7 @@ namespace {
 #endif
 
 constexpr int kGuard = 16;  // poisoned ints after every slot and warp region
+int failures = 0;
 
 struct Csr {
     int v = 0;
@@ -109,6 +110,7 @@ std::vector<Sched> motif_schedules(const Csr& g, int k, bool iep, int stride) {
 
 struct Knobs {
     int blocks = 2, wpb = 4, chunk = 2, stage_cap = 64, leaf = 1, pair = 0, split = 0, pair_log2 = 13;
+    int bm_min = 0;  // > 0: leaf bitmaps for fixed sets of at least this size
     unsigned long long stripes = 1, stripe = 0;
 };
 
@@ -142,6 +144,8 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     unsigned long long params[2] = {k.stripes, k.stripe};
     std::vector<unsigned long long> tables;
     if (k.pair) tables.assign((size_t)warps << k.pair_log2, 0ull);
+    const int bm_words = k.bm_min > 0 ? (g.v + 31) / 32 : 0;
+    std::vector<unsigned> bitmaps((size_t)warps * 2 * bm_words, 0u);
     DonationArea* don = k.split > 0 ? new DonationArea() : nullptr;
     if (don) std::memset((void*)don, 0, sizeof(DonationArea));
     const size_t smem = sizeof(WarpState) * k.wpb + sizeof(int) * 2 * (size_t)k.stage_cap * k.wpb;
@@ -162,7 +166,8 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
                 auto body = [&](int) {
                     match_kernel<false>(pairs.data(), n, cursors.data(), out.data(), scratch.data(), per_warp, k.chunk,
                                         params, k.leaf, k.stage_cap, k.pair, k.pair ? tables.data() : nullptr, k.pair_log2, don,
-                                        k.split, stats.data());
+                                        k.split, bm_words ? bitmaps.data() : nullptr, bm_words, k.bm_min,
+                                        stats.data());
                 };
                 gpm_emu::run_warp(*w, body);
                 delete w;
@@ -185,6 +190,12 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
             ASAN_UNPOISON_MEMORY_REGION(base + (size_t)s * cap + (cap - kGuard), kGuard * 4);
         ASAN_UNPOISON_MEMORY_REGION(base + (size_t)nslots * cap, kGuard * 4);
     }
+    for (unsigned w : bitmaps)
+        if (w) {
+            std::printf("bitmap left dirty after the launch\n");
+            ++failures;
+            break;
+        }
     if (g_check[0]) {
         std::fprintf(stderr, "internal check %llu: %lld %lld %lld %lld %lld %lld\n", g_check[0], (long long)g_check[1],
                      (long long)g_check[2], (long long)g_check[3], (long long)g_check[4], (long long)g_check[5],
@@ -195,8 +206,6 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     for (int i = 0; i < n; ++i) raw[i] = (__int128)(((unsigned __int128)out[2 * i + 1] << 64) | out[2 * i]);
     return raw;
 }
-
-int failures = 0;
 
 void expect_oracle(const char* what, const Csr& g, const std::vector<Sched>& ss, const Knobs& k) {
     const std::vector<__int128> raw = launch(g, ss, k);
@@ -249,6 +258,23 @@ void case_quick() {
         k.leaf = leaf;
         expect_oracle("rmat7", g, ss, k);
     }
+    Knobs k;  // leaf bitmaps for every fixed set that does not fit the stage
+    k.split = 1;
+    k.stage_cap = 8;
+    k.bm_min = 1;
+    expect_oracle("rmat7 bitmaps", g, ss, k);
+}
+
+// hub leaf levels longer than one slice: batched leaves taken in pieces
+void case_leafslices() {
+    const Csr g = rmat(8, 12, 31);
+    std::vector<Sched> ss = motif_schedules(g, 5, true, 3);
+    Knobs k;
+    k.split = 1;
+    k.leaf = 1;
+    expect_oracle("rmat8 leaf slices", g, ss, k);
+    k.bm_min = 16;
+    expect_oracle("rmat8 leaf slices + bitmaps", g, ss, k);
 }
 
 void case_pair() {
@@ -300,6 +326,7 @@ int main(int argc, char** argv) {
     for (const std::string& c : cases) {
         if (c == "quick") case_quick();
         else if (c == "donation") case_donation();
+        else if (c == "leafslices") case_leafslices();
         else if (c == "pair") case_pair();
         else if (c == "stripes") case_stripes();
         else {

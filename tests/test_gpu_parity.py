@@ -319,3 +319,17 @@ def test_stripes_do_not_depend_on_chunk(engine):
         opts = {"raw_sums": 1, "stripes": 8, "stripe": 5, "chunk": chunk}
         runs.append(_with_options(opts, lambda: gp.batch_count(pairs, scheds)))
     assert runs[0] == runs[1] == runs[2]
+
+
+def test_leaf_bitmaps_match_oracle(engine, oracle):
+    # membership in large fixed leaf sets through per-warp bitmaps: forced on
+    # for every set that does not fit a tiny stage, and off
+    g = gp.rmat(11, 16, 0.57, 0.19, 0.19, 33)
+    tri = g.triangle_counting_mt()
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
+    scheds += [gp.Schedule(p, 1, 1, False, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()[9::5]]
+    want = [oracle.count(g, s) for s in scheds]
+    pairs = [g] * len(scheds)
+    for opts in ({"bitmap_min": 1, "stage_max": 16}, {"bitmap_min": 1, "stage_max": 16, "split": 1},
+                 {"bitmap_min": 0}):
+        assert _with_options(opts, lambda: gp.batch_count(pairs, scheds)) == want, opts
