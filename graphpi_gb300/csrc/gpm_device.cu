@@ -911,6 +911,138 @@ GPM_API int gpm_batch_exec_destroy(gpm_batch_exec* exec) {
     return GPM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Counting without any device allocation.
+//
+// Some callers cannot call cudaMalloc: programs whose device memory is
+// reserved by another allocator (a framework's caching allocator or a fixed
+// arena that owns the GPU, so a cudaMalloc fails or fragments its pool), and
+// latency-critical loops that cannot afford cudaMalloc/cudaFree's implicit
+// device synchronisation.  gpm_count_noalloc serves them with the scratch below: a
+// file-scope device array that every GPU loading this library holds until
+// the process exits.  Host code cannot use the array's name as an address;
+// the device address comes from cudaGetSymbolAddress, once per device.
+
+namespace gpm {
+
+constexpr size_t kNoAllocBytes = 64ull << 20;  // 64 MiB
+constexpr size_t kNoAllocHeader = 8192;        // control words, pair, plan
+static_assert(512 + sizeof(DevPlan) <= kNoAllocHeader, "plan does not fit the header");
+static_assert(sizeof(PairDesc) <= 256, "pair does not fit the header");
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+static void* g_noalloc_addr[64] = {nullptr};
+static std::mutex g_noalloc_mu;
+
+__global__ void max_degree_kernel(const unsigned* __restrict__ rowptr, int v_cnt, unsigned* __restrict__ out) {
+    unsigned m = 0;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < v_cnt; v += (long long)gridDim.x * blockDim.x)
+        m = max(m, rowptr[v + 1] - rowptr[v]);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) m = max(m, __shfl_xor_sync(kFull, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+}  // namespace gpm
+
+GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int32_t* d_col, const int64_t* tables,
+                              int32_t n_words, gpm_u128* out) {
+    clear_error();
+    if (v_cnt < 1 || !d_rowptr || !d_col || !tables || !out) {
+        set_error("gpm_count_noalloc: need v_cnt >= 1, device CSR pointers, tables and out");
+        return GPM_ERR_INVALID_ARG;
+    }
+    DevPlan hp;
+    int rc = compile_plan(tables, n_words, &hp);
+    if (rc) return rc;
+    int dev = 0, sms = 0;
+    GPM_CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("gpm_count_noalloc: device %d out of range", dev);
+        return GPM_ERR_NO_DEVICE;
+    }
+    GPM_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    unsigned char* base = nullptr;
+    {
+        // set-up once per device, with that device current
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                set_error("gpm_count_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+                return GPM_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = p;
+        }
+        base = (unsigned char*)g_noalloc_addr[dev];
+    }
+    cudaStream_t st = cudaStreamPerThread;
+    // control words: [0] work cursor, [1..2] 128-bit sum, [3..4] stats,
+    // [5..6] stripes/stripe, [7] max degree
+    unsigned long long* ctrl = (unsigned long long*)base;
+    PairDesc* d_pair = (PairDesc*)(base + 256);
+    DevPlan* d_plan = (DevPlan*)(base + 512);
+    int* warp_scratch = (int*)(base + kNoAllocHeader);
+    const unsigned long long init[8] = {0, 0, 0, 0, 0, 1, 0, 0};
+    GPM_CK(cudaMemcpyAsync(ctrl, init, sizeof init, cudaMemcpyHostToDevice, st));
+    max_degree_kernel<<<sms * 4, 256, 0, st>>>(d_rowptr, v_cnt, (unsigned*)(ctrl + 7));
+    GPM_CK(cudaGetLastError());
+    uint32_t e_cnt = 0, maxdeg = 0;
+    GPM_CK(cudaMemcpyAsync(&e_cnt, d_rowptr + v_cnt, sizeof e_cnt, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaMemcpyAsync(&maxdeg, ctrl + 7, sizeof maxdeg, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    // size the grid to what the array holds
+    const Options& o = options();
+    const int wpb = (int)o.warps_per_block;
+    const long long cap = std::max<long long>(1, maxdeg);
+    const long long per_warp = (long long)hp.nslots * cap;
+    const long long fit = (long long)((kNoAllocBytes - kNoAllocHeader) / ((size_t)per_warp * sizeof(int)));
+    const long long want = (long long)sms * o.blocks_per_sm * wpb;
+    const long long warps = std::min(want, fit) / wpb * wpb;
+    if (warps < wpb) {
+        set_error("gpm_count_noalloc: one block of %d warps needs %lld bytes of scratch (%d sets x largest degree %lld "
+                  "x 4 bytes per warp); the allocation-free scratch holds %zu bytes: use gpm_count",
+                  wpb, (long long)wpb * per_warp * 4, hp.nslots, cap, kNoAllocBytes - kNoAllocHeader);
+        return GPM_ERR_UNSUPPORTED;
+    }
+    PairDesc pd;
+    pd.g.rowptr = d_rowptr;
+    pd.g.col = d_col;
+    pd.g.v_cnt = v_cnt;
+    pd.g.pad_ = 0;
+    pd.g.e_cnt = e_cnt;
+    pd.plan = d_plan;
+    pd.ntasks = hp.T == 1 ? (unsigned long long)v_cnt : (unsigned long long)e_cnt;
+    pd.cap = (int)cap;
+    pd.pad_ = 0;
+    GPM_CK(cudaMemcpyAsync(d_pair, &pd, sizeof pd, cudaMemcpyHostToDevice, st));
+    GPM_CK(cudaMemcpyAsync(d_plan, &hp, sizeof hp, cudaMemcpyHostToDevice, st));
+    const int alpha4[3] = {(int)o.merge_alpha4[0], (int)o.merge_alpha4[1], (int)o.merge_alpha4[2]};
+    GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, st));
+    const int stage_cap = (int)o.stage_max;
+    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
+    GPM_CK(cudaFuncSetAttribute(match_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    match_kernel<false><<<(unsigned)(warps / wpb), wpb * 32, smem, st>>>(
+        d_pair, 1, ctrl, ctrl + 1, warp_scratch, per_warp, (int)o.chunk, ctrl + 5, (int)o.leaf_batch, stage_cap,
+        0, nullptr, 0, nullptr, 0, nullptr, 0, 0, ctrl + 3);
+    GPM_CK(cudaGetLastError());
+    unsigned long long raw[2] = {0, 0};
+    GPM_CK(cudaMemcpyAsync(raw, ctrl + 1, sizeof raw, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    rc = take_check("gpm_count_noalloc");
+    if (rc) return rc;
+    const unsigned __int128 u = ((unsigned __int128)raw[1] << 64) | raw[0];
+    if ((__int128)u < 0) {
+        set_error("gpm_count_noalloc: negative total (128-bit overflow)");
+        return GPM_ERR_OVERFLOW;
+    }
+    const unsigned __int128 q = u / (unsigned __int128)hp.redundancy;
+    out->lo = (uint64_t)q;
+    out->hi = (uint64_t)(q >> 64);
+    return GPM_OK;
+}
+
 GPM_API int gpm_last_launch_stats(double* kernel_ms, int64_t* launches, uint64_t* algo_bytes) {
     if (kernel_ms) *kernel_ms = t_ms;
     if (launches) *launches = t_launches;

@@ -61,6 +61,7 @@ SIGNATURES = {
     "gpm_batch_exec_run": (I32, [C.POINTER(P), I32, P, P, P]),
     "gpm_batch_exec_destroy": (I32, [P]),
     "gpm_count_host": (I32, [I32, P, P, I32, P, P, P]),
+    "gpm_count_noalloc": (I32, [I32, P, P, P, I32, C.POINTER(U128)]),
     "gpm_set_option": (I32, [C.c_char_p, I64]),
     "gpm_get_option": (I32, [C.c_char_p, PI64]),
     "gpm_last_launch_stats": (I32, [C.POINTER(C.c_double), PI64, PU64]),

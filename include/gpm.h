@@ -231,6 +231,27 @@ GPM_API int gpm_mlp_gradients(gpm_mlp* m, const float* X, const float* T, int32_
 GPM_API int gpm_mlp_train(gpm_mlp* m, const float* X, const float* T, int32_t n_rows, int32_t epochs, float lr,
                           float weight_decay, float* final_loss);
 
+/* Counting that allocates nothing on the device.  No counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc — programs whose
+ * GPU memory is owned by another allocator (a framework's caching allocator
+ * or a fixed arena, where a cudaMalloc fails or fragments the pool), and
+ * latency-critical loops that cannot take cudaMalloc/cudaFree's implicit
+ * device synchronisation.
+ * The caller passes the CSR already in device memory (layout of
+ * gpm_graph_create, counted on the ids as given), schedule tables (host) and
+ * the result location (host).  Scratch is a 64 MiB file-scope device array
+ * that every GPU loading the library holds until exit; the grid is sized to
+ * it, and a pattern/graph whose per-warp sets (scratch sets x largest degree
+ * x 4 bytes) do not fit one block returns GPM_ERR_UNSUPPORTED ("use
+ * gpm_count").  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  Work runs on the per-thread default stream and the call waits
+ * for it.  All calls share the one array: it keeps the last call's contents
+ * (each call clears the words that must start at zero), and calls that
+ * overlap on the GPU — from several host threads — race on it. */
+GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int32_t* d_col,
+                              const int64_t* tables, int32_t n_words, gpm_u128* out);
+
 /* ------------------------------------------------------------------ */
 /* tuning                                                              */
 /* ------------------------------------------------------------------ */
