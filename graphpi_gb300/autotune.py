@@ -165,3 +165,51 @@ def autotune(graph, schedules, stripes: int = 1024, sample_stripes: int = 2, rep
     best["_trials"] = len(history)
     best["_default_ms"] = history[0][1]
     return best
+
+
+TUNED = Path(__file__).resolve().parent / "tuned" / "tables.json"
+
+
+def apply_stored(graph, schedules, path: str | Path = TUNED) -> dict | None:
+    """Installs the table tuned for this graph and pattern set, if one is
+    stored; returns it (None when there is none)."""
+    table = load(path, signature(graph, schedules))
+    if table:
+        apply({k: v for k, v in table.items() if not k.startswith("_")})
+    return table
+
+
+def main(argv: list[str] | None = None) -> dict:
+    """Tunes the knobs for the 29 motifs (3-5 vertices) on an R-MAT graph and
+    stores the table under its signature.
+
+        python -m graphpi_gb300.autotune --scale 22 --out graphpi_gb300/tuned/tables.json
+    """
+    import argparse
+
+    from . import workloads
+    from .api import Schedule, motifs_3_to_5
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--stripes", type=int, default=1 << 26, help="the sample is a few of this many stripes")
+    ap.add_argument("--samples", type=int, default=4)
+    ap.add_argument("--budget", type=float, default=120.0, help="seconds")
+    ap.add_argument("--out", default=str(TUNED))
+    a = ap.parse_args(argv)
+    g = workloads.rmat_s22() if (a.scale, a.seed) == (22, 3) else workloads.rmat_scale(a.scale, a.seed)
+    tri = g.triangle_counting_mt()
+    scheds = [Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in motifs_3_to_5()]
+    table = autotune(g, scheds, stripes=a.stripes, sample_stripes=a.samples, repeats=1, budget_s=a.budget,
+                     verbose=True)
+    table["_graph"] = f"rmat s{a.scale} seed {a.seed}"
+    table["_sample"] = f"{a.samples} of {a.stripes} stripes"
+    Path(a.out).parent.mkdir(parents=True, exist_ok=True)
+    save(table, a.out, signature(g, scheds))
+    print(json.dumps(table, indent=1, sort_keys=True))
+    return table
+
+
+if __name__ == "__main__":
+    main()

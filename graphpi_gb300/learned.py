@@ -213,3 +213,52 @@ def evaluate(rows: list[dict], model: CostModel) -> dict:
     tot["analytic_over_best"] = tot["analytic"] / max(tot["best"], 1e-9)
     tot["per_pattern"] = per
     return tot
+
+
+def main(argv: list[str] | None = None) -> dict:
+    """Trains the cost model on runtimes measured on one R-MAT graph and
+    reports, for held-out patterns on another, the measured runtime of the
+    MLP's choice, of the analytic model's choice and of the best candidate.
+
+        python -m graphpi_gb300.learned --train-scale 16 --eval-scale 18
+    """
+    import argparse
+    import json
+
+    from . import workloads
+    from .api import MotifGenerator
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train-scale", type=int, default=16)
+    ap.add_argument("--eval-scale", type=int, default=18)
+    ap.add_argument("--six-stride", type=int, default=8, help="every k-th of the 112 six-vertex motifs")
+    ap.add_argument("--candidates", type=int, default=12)
+    ap.add_argument("--epochs", type=int, default=3000)
+    ap.add_argument("--out", default="")
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    pats = MotifGenerator(5).generate() + MotifGenerator(6).generate()[::a.six_stride]
+    train, held = pats[::2], pats[1::2]
+    g_tr = workloads.rmat_scale(a.train_scale, 2)
+    rows_tr = collect(g_tr, train, max_candidates=a.candidates)
+    g_ev = workloads.rmat_scale(a.eval_scale, 4)
+    rows_ev = collect(g_ev, held, max_candidates=a.candidates)
+    model = CostModel(hidden=64, seed=1)
+    loss = model.fit(rows_tr, epochs=a.epochs)
+    ev = evaluate(rows_ev, model)
+    res = {"train_graph": f"rmat s{a.train_scale}", "eval_graph": f"rmat s{a.eval_scale}",
+           "train_rows": len(rows_tr), "eval_rows": len(rows_ev), "train_loss": loss,
+           "mlp_over_best": ev["mlp_over_best"], "analytic_over_best": ev["analytic_over_best"],
+           "mlp_ms": ev["mlp"], "analytic_ms": ev["analytic"], "best_ms": ev["best"],
+           "per_pattern": ev["per_pattern"], "seconds": time.time() - t0}
+    model.close()
+    text = json.dumps(res, indent=1)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(text)
+    print(text)
+    return res
+
+
+if __name__ == "__main__":
+    main()

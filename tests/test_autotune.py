@@ -28,3 +28,17 @@ def test_autotune_keeps_counts(engine, oracle):
         assert gp.batch_count([g] * len(scheds), scheds) == [oracle.count(g, s) for s in scheds]
     finally:
         autotune.apply(before)
+
+
+def test_stored_table_applies_by_signature(engine, tmp_path):
+    g = gp.rmat(8, 8, 0.57, 0.19, 0.19, 3)
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, 100) for p in gp.motifs_3_to_5()[:3]]
+    p = tmp_path / "tables.json"
+    autotune.save({"chunk": 3, "_ms": 1.0}, p, autotune.signature(g, scheds))
+    before = autotune.current()
+    try:
+        assert autotune.apply_stored(g, scheds[:2], p) is None  # another pattern set
+        t = autotune.apply_stored(g, scheds, p)
+        assert t["chunk"] == 3 and gp.get_option("chunk") == 3
+    finally:
+        autotune.apply(before)
