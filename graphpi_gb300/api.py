@@ -474,9 +474,24 @@ def chung_lu(n: int, avg_degree: float, gamma: float, max_degree: int = 0, seed:
     return Graph(nv.value, vertex, edge)
 
 
-def from_edges(v_cnt: int, src, dst) -> Graph:
+def from_edges(v_cnt: int, src, dst, on_device: bool = False) -> Graph:
+    """Graph from undirected edges (self loops and duplicates dropped).
+    on_device: sort and deduplicate on the GPU (gpm_graph_from_edges); the
+    device copy is kept and the host CSR downloaded."""
     s = np.ascontiguousarray(src, dtype=np.int32)
     d = np.ascontiguousarray(dst, dtype=np.int32)
+    if on_device:
+        h = C.c_void_p()
+        check(lib().gpm_graph_from_edges(v_cnt, len(s), s.ctypes.data, d.ctypes.data, 1, C.byref(h)),
+              "gpm_graph_from_edges")
+        e = C.c_int64()
+        check(lib().gpm_graph_stats(h, None, C.byref(e), None, None), "gpm_graph_stats")
+        vertex = np.zeros(v_cnt + 1, dtype=np.uint32)
+        edge = np.zeros(max(1, e.value), dtype=np.int32)
+        check(lib().gpm_graph_download(h, vertex.ctypes.data, edge.ctypes.data), "gpm_graph_download")
+        g = Graph(v_cnt, vertex, edge[:e.value])
+        g._dev = h
+        return g
     rp, cl = C.POINTER(C.c_uint32)(), C.POINTER(C.c_int32)()
     check(lib().gpm_csr_from_edges(v_cnt, len(s), s.ctypes.data, d.ctypes.data, C.byref(rp), C.byref(cl)),
           "from_edges")

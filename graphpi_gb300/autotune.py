@@ -12,6 +12,8 @@ Knobs (gpm_set_option):
   chunk                     first-level tasks per work-queue grab
   warps_per_block           warps per persistent block
   blocks_per_sm             persistent blocks per SM
+  min_blocks                3: the kernel variant compiled for three 8-warp
+                            blocks per SM (80 registers) instead of 122
   stage_max                 largest fixed set staged in shared memory (ints)
   leaf_batch                batched deepest loop level on/off
   pair_leaf                 pair sums over the last two loops on/off
@@ -38,6 +40,7 @@ SPACE = {
     "chunk": [1, 2, 4, 8, 16, 32],
     "warps_per_block": [4, 8, 16],
     "blocks_per_sm": [1, 2, 3],
+    "min_blocks": [1, 3],
     "stage_max": [0, 256, 1024, 2048],
     "leaf_batch": [0, 1],
     "pair_leaf": [0, 1],
@@ -147,7 +150,12 @@ def autotune(graph, schedules, stripes: int = 1024, sample_stripes: int = 2, rep
                     cand = dict(best)
                     cand[knob] = v
                     apply(cand)
-                    ms = measure()
+                    try:
+                        ms = measure()
+                    except native.GpmError as e:  # a shape this device cannot launch
+                        if verbose:
+                            print(f"[autotune] {knob}={v}: skipped ({e})", flush=True)
+                        continue
                     history.append((cand, ms))
                     if verbose:
                         print(f"[autotune] {knob}={v}: {ms:.2f} ms (best {best_ms:.2f})", flush=True)

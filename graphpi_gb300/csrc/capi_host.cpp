@@ -687,6 +687,13 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "pair_leaf") slot = &o.pair_leaf, lo = 0, hi = 1;
     else if (k == "pair_log2") slot = &o.pair_log2, lo = 0, hi = 24;
     else if (k == "bitmap_min") slot = &o.bitmap_min, lo = 0, hi = 1 << 30;
+    else if (k == "min_blocks") {
+        if (value != 1 && value != 3) {
+            set_error("gpm_set_option: min_blocks is 1 or 3");
+            return GPM_ERR_INVALID_ARG;
+        }
+        slot = &o.min_blocks, lo = 1, hi = 3;
+    }
     else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
     else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;
     else if (k == "stripe") slot = &o.stripe, lo = 0, hi = (1 << 30) - 1;
@@ -721,6 +728,7 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "pair_leaf") *value = o.pair_leaf;
     else if (k == "pair_log2") *value = o.pair_log2;
     else if (k == "bitmap_min") *value = o.bitmap_min;
+    else if (k == "min_blocks") *value = o.min_blocks;
     else if (k == "split") *value = o.split;
     else if (k == "stripes") *value = o.stripes;
     else if (k == "stripe") *value = o.stripe;

@@ -239,6 +239,8 @@ static int take_check(const char* where) {
 
 static unsigned validate_csr(DeviceCtx* c, const GraphView& v, int* rc);
 
+
+
 static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     const int V = g->v_cnt;
     const unsigned E = (unsigned)g->e_cnt;
@@ -362,6 +364,7 @@ struct LaunchSetup {
     int split_min = 0;
     int bm_words = 0;  // words per leaf bitmap (0: no bitmaps)
     int bm_min = 0;
+    int min_blocks = 1;  // kernel variant: 1 or 3 resident blocks per SM
     bool count_bytes = false;
 };
 
@@ -398,7 +401,14 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
     ls.stage_cap = (int)o.stage_max;
     ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)ls.stage_cap * ls.wpb;
     ls.count_bytes = o.count_bytes != 0;
-    const void* kfn = ls.count_bytes ? (const void*)match_kernel<true> : (const void*)match_kernel<false>;
+    ls.min_blocks = (o.min_blocks == 3 && !ls.count_bytes) ? 3 : 1;
+    if (ls.min_blocks == 3 && ls.wpb > 8) {
+        set_error("min_blocks=3 needs warps_per_block <= 8 (got %d)", ls.wpb);
+        return GPM_ERR_INVALID_ARG;
+    }
+    const void* kfn = ls.count_bytes       ? (const void*)match_kernel<true, 1>
+                      : ls.min_blocks == 3 ? (const void*)match_kernel<false, 3>
+                                           : (const void*)match_kernel<false, 1>;
     GPM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
     // a persistent grid: no more blocks than can be resident at once
     int occ = 0;
@@ -407,7 +417,8 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         set_error("launch shape does not fit an SM: %d warps per block, %zu bytes of shared memory", ls.wpb, ls.smem);
         return GPM_ERR_INVALID_ARG;
     }
-    ls.blocks = (long long)c->num_sms * std::min<long long>(o.blocks_per_sm, occ);
+    // the 3-block variant launches three blocks per SM when they fit
+    ls.blocks = (long long)c->num_sms * std::min<long long>(std::max<long long>(o.blocks_per_sm, ls.min_blocks), occ);
     ls.per_warp = (long long)nslots * cap;
     // shrink the grid when the per-warp scratch would not fit in free memory
     size_t free_b = 0, total_b = 0;
@@ -503,14 +514,16 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
         const cudaError_t e = cudaMemsetAsync(bitmaps, 0, bitmap_bytes(ls), st);
         if (e != cudaSuccess) return e;
     }
+#define GPM_MATCH_ARGS                                                                                        \
+    d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on, tables, \
+        ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, stats
     if (ls.count_bytes)
-        match_kernel<true><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
-            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
-            tables, ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, stats);
+        match_kernel<true, 1><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
+    else if (ls.min_blocks == 3)
+        match_kernel<false, 3><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
     else
-        match_kernel<false><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(
-            d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on,
-            tables, ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, stats);
+        match_kernel<false, 1><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
+#undef GPM_MATCH_ARGS
     return cudaGetLastError();
 }
 
@@ -576,6 +589,29 @@ static int finish_counts(int n, const gpm_plan* const* plans, const unsigned lon
     return GPM_OK;
 }
 
+// Validates a freshly built device CSR and relabels it by degree.
+static int finish_graph(DeviceCtx* c, gpm_graph* g, bool relabel, const char* who) {
+    cudaStream_t st = c->stream;
+    DevBuf d_flags;
+    GPM_CK(cudaMalloc(&d_flags.p, sizeof(unsigned)));
+    GPM_CK(cudaMemsetAsync(d_flags.p, 0, sizeof(unsigned), st));
+    validate_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), (unsigned*)d_flags.p);
+    unsigned flags = 0;
+    GPM_CK(cudaMemcpyAsync(&flags, d_flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        set_error("%s: validation failed: %s", who, cudaGetErrorString(e));
+        return GPM_ERR_CUDA;
+    }
+    if (flags) {
+        set_error("%s: malformed CSR (%s%s%s%s%s)", who, flags & 1 ? "offsets " : "",
+                  flags & 2 ? "ids-out-of-range " : "", flags & 4 ? "self-loops " : "",
+                  flags & 8 ? "unsorted-or-duplicate " : "", flags & 16 ? "asymmetric" : "");
+        return GPM_ERR_INVALID_ARG;
+    }
+    return relabel_graph(c, g, relabel);
+}
+
 }  // namespace gpm
 
 using namespace gpm;
@@ -634,27 +670,146 @@ GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_
         set_error("gpm_graph_create: upload failed: %s", cudaGetErrorString(cudaGetLastError()));
         return fail(GPM_ERR_CUDA);
     }
-    unsigned* d_flags = nullptr;
-    if (cudaMalloc(&d_flags, sizeof(unsigned)) != cudaSuccess) return fail(GPM_ERR_OOM);
-    cudaMemsetAsync(d_flags, 0, sizeof(unsigned), st);
-    validate_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), d_flags);
-    unsigned flags = 0;
-    cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-    cudaError_t e = cudaStreamSynchronize(st);
-    cudaFree(d_flags);
-    if (e != cudaSuccess) {
-        set_error("gpm_graph_create: validation failed: %s", cudaGetErrorString(e));
-        return fail(GPM_ERR_CUDA);
-    }
-    if (flags) {
-        set_error("gpm_graph_create: malformed CSR (%s%s%s%s%s)", flags & 1 ? "offsets " : "",
-                  flags & 2 ? "ids-out-of-range " : "", flags & 4 ? "self-loops " : "",
-                  flags & 8 ? "unsorted-or-duplicate " : "", flags & 16 ? "asymmetric" : "");
-        return fail(GPM_ERR_INVALID_ARG);
-    }
-    int rc = relabel_graph(c, g, relabel != 0);
+    const int rc = finish_graph(c, g, relabel != 0, "gpm_graph_create");
     if (rc) return fail(rc);
     *out = g;
+    return GPM_OK;
+}
+
+// Edge list -> CSR on the GPU (the steps of src/dataloader.cpp:129-160:
+// symmetrise, drop self loops, sort, deduplicate, offsets).  Keys are
+// (u << 32 | v) for both directions; a self loop or an id out of range
+// becomes the sentinel ~0, which sorts last.
+__global__ void edge_keys_kernel(const int* __restrict__ src, const int* __restrict__ dst, long long m, int v_cnt,
+                                 unsigned long long* __restrict__ keys, unsigned* __restrict__ bad) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+        const int u = src[i], v = dst[i];
+        unsigned long long k0 = ~0ull, k1 = ~0ull;
+        if ((unsigned)u >= (unsigned)v_cnt || (unsigned)v >= (unsigned)v_cnt) {
+            atomicOr(bad, 1u);
+        } else if (u != v) {
+            k0 = ((unsigned long long)(unsigned)u << 32) | (unsigned)v;
+            k1 = ((unsigned long long)(unsigned)v << 32) | (unsigned)u;
+        }
+        keys[2 * i] = k0;
+        keys[2 * i + 1] = k1;
+    }
+}
+
+// rowptr[v] = first key with source >= v; col = low halves
+__global__ void keys_to_csr_kernel(const unsigned long long* __restrict__ keys, unsigned long long e, int v_cnt,
+                                   unsigned* __restrict__ rowptr, int* __restrict__ col) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v <= v_cnt; v += stride) {
+        const unsigned long long key = (unsigned long long)v << 32;
+        unsigned long long lo = 0, hi = e;
+        while (lo < hi) {
+            const unsigned long long mid = (lo + hi) >> 1;
+            if (keys[mid] < key) lo = mid + 1;
+            else hi = mid;
+        }
+        rowptr[v] = (unsigned)lo;
+    }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)e; i += stride)
+        col[i] = (int)(unsigned)(keys[i] & 0xffffffffull);
+}
+
+GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, const int32_t* dst, int32_t relabel,
+                                 gpm_graph** out) {
+    clear_error();
+    if (!out || v_cnt < 1 || m < 0 || (m > 0 && (!src || !dst))) {
+        set_error("gpm_graph_from_edges: need v_cnt >= 1, m >= 0, src, dst and out");
+        return GPM_ERR_INVALID_ARG;
+    }
+    if ((unsigned long long)m * 2 >= (1ull << 32)) {
+        set_error("gpm_graph_from_edges: %lld edges exceed 32-bit offsets", (long long)m);
+        return GPM_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> lk(c->mu);
+    cudaStream_t st = c->stream;
+    const size_t n2 = (size_t)std::max<int64_t>(1, 2 * m);
+    DevBuf d_src, d_dst, keys, keys2, uniq, nsel, bad, tmp;
+    GPM_CK(cudaMalloc(&d_src.p, sizeof(int) * std::max<int64_t>(m, 1)));
+    GPM_CK(cudaMalloc(&d_dst.p, sizeof(int) * std::max<int64_t>(m, 1)));
+    GPM_CK(cudaMalloc(&keys.p, sizeof(unsigned long long) * n2));
+    GPM_CK(cudaMalloc(&keys2.p, sizeof(unsigned long long) * n2));
+    GPM_CK(cudaMalloc(&uniq.p, sizeof(unsigned long long) * n2));
+    GPM_CK(cudaMalloc(&nsel.p, sizeof(unsigned long long)));
+    GPM_CK(cudaMalloc(&bad.p, sizeof(unsigned)));
+    GPM_CK(cudaMemsetAsync(bad.p, 0, sizeof(unsigned), st));
+    if (m > 0) {
+        GPM_CK(cudaMemcpyAsync(d_src.p, src, sizeof(int) * m, cudaMemcpyHostToDevice, st));
+        GPM_CK(cudaMemcpyAsync(d_dst.p, dst, sizeof(int) * m, cudaMemcpyHostToDevice, st));
+        edge_keys_kernel<<<c->num_sms * 8, 256, 0, st>>>((const int*)d_src.p, (const int*)d_dst.p, m, v_cnt,
+                                                         (unsigned long long*)keys.p, (unsigned*)bad.p);
+        GPM_CK(cudaGetLastError());
+    }
+    const int n2i = (int)std::min<size_t>(n2, (size_t)INT_MAX);
+    size_t tb_sort = 0, tb_uniq = 0;
+    GPM_CK(cub::DeviceRadixSort::SortKeys(nullptr, tb_sort, (unsigned long long*)keys.p, (unsigned long long*)keys2.p,
+                                          n2i, 0, 64, st));
+    GPM_CK(cub::DeviceSelect::Unique(nullptr, tb_uniq, (unsigned long long*)keys2.p, (unsigned long long*)uniq.p,
+                                     (unsigned long long*)nsel.p, n2i, st));
+    GPM_CK(cudaMalloc(&tmp.p, std::max<size_t>(std::max(tb_sort, tb_uniq), 1)));
+    unsigned long long h_n = 0, h_last = ~0ull;
+    unsigned h_bad = 0;
+    if (m > 0) {
+        GPM_CK(cub::DeviceRadixSort::SortKeys(tmp.p, tb_sort, (unsigned long long*)keys.p,
+                                              (unsigned long long*)keys2.p, n2i, 0, 64, st));
+        GPM_CK(cub::DeviceSelect::Unique(tmp.p, tb_uniq, (unsigned long long*)keys2.p, (unsigned long long*)uniq.p,
+                                         (unsigned long long*)nsel.p, n2i, st));
+        GPM_CK(cudaMemcpyAsync(&h_n, nsel.p, sizeof h_n, cudaMemcpyDeviceToHost, st));
+    }
+    GPM_CK(cudaMemcpyAsync(&h_bad, bad.p, sizeof h_bad, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    if (h_bad) {
+        set_error("gpm_graph_from_edges: an edge names a vertex outside [0, %d)", v_cnt);
+        return GPM_ERR_INVALID_ARG;
+    }
+    if (h_n > 0) {
+        GPM_CK(cudaMemcpy(&h_last, (unsigned long long*)uniq.p + (h_n - 1), sizeof h_last, cudaMemcpyDeviceToHost));
+        if (h_last == ~0ull) --h_n;  // the self-loop sentinel
+    }
+    gpm_graph* g = new gpm_graph();
+    g->v_cnt = v_cnt;
+    g->e_cnt = h_n;
+    g->device = c->device;
+    if (cudaMalloc(&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
+        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(h_n, 1)) != cudaSuccess) {
+        if (g->rowptr) cudaFree(g->rowptr);
+        delete g;
+        set_error("gpm_graph_from_edges: out of device memory for %llu edges", h_n);
+        return GPM_ERR_OOM;
+    }
+    keys_to_csr_kernel<<<c->num_sms * 8, 256, 0, st>>>((const unsigned long long*)uniq.p, h_n, v_cnt, g->rowptr,
+                                                       g->col);
+    const int rc = finish_graph(c, g, relabel != 0, "gpm_graph_from_edges");
+    if (rc) {
+        if (g->orig_rowptr && g->orig_rowptr != g->rowptr) cudaFree(g->orig_rowptr);
+        if (g->orig_col && g->orig_col != g->col) cudaFree(g->orig_col);
+        cudaFree(g->rowptr);
+        cudaFree(g->col);
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return GPM_OK;
+}
+
+GPM_API int gpm_graph_download(const gpm_graph* g, uint32_t* rowptr, int32_t* col) {
+    clear_error();
+    if (!g || !rowptr || (g->e_cnt && !col)) {
+        set_error("gpm_graph_download: null argument");
+        return GPM_ERR_INVALID_ARG;
+    }
+    const uint32_t* rp = g->orig_rowptr ? g->orig_rowptr : g->rowptr;
+    const int32_t* cl = g->orig_col ? g->orig_col : g->col;
+    GPM_CK(cudaMemcpy(rowptr, rp, sizeof(uint32_t) * ((size_t)g->v_cnt + 1), cudaMemcpyDeviceToHost));
+    if (g->e_cnt) GPM_CK(cudaMemcpy(col, cl, sizeof(int32_t) * g->e_cnt, cudaMemcpyDeviceToHost));
     return GPM_OK;
 }
 
@@ -1022,8 +1177,8 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, st));
     const int stage_cap = (int)o.stage_max;
     const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
-    GPM_CK(cudaFuncSetAttribute(match_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    match_kernel<false><<<(unsigned)(warps / wpb), wpb * 32, smem, st>>>(
+    GPM_CK(cudaFuncSetAttribute(match_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    match_kernel<false, 1><<<(unsigned)(warps / wpb), wpb * 32, smem, st>>>(
         d_pair, 1, ctrl, ctrl + 1, warp_scratch, per_warp, (int)o.chunk, ctrl + 5, (int)o.leaf_batch, stage_cap,
         0, nullptr, 0, nullptr, 0, nullptr, 0, 0, ctrl + 3);
     GPM_CK(cudaGetLastError());

@@ -1140,8 +1140,10 @@ struct WarpCtx {
     }
 };
 
-template <bool kBytes>
-__global__ void __launch_bounds__(512, 1) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
+// kMinBlocks 1: any block up to 16 warps; 3: blocks of at most 8 warps, three
+// resident per SM (the register budget drops to 80, with a few spills)
+template <bool kBytes, int kMinBlocks>
+__global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
                                                     unsigned long long* __restrict__ cursors,
                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
                                                     long long scratch_per_warp, int chunk,

@@ -44,6 +44,8 @@ SIGNATURES = {
     "gpm_last_error": (C.c_char_p, []),
     "gpm_set_device": (I32, [I32]),
     "gpm_graph_create": (I32, [I32, P, P, I32, C.POINTER(P)]),
+    "gpm_graph_from_edges": (I32, [I32, C.c_int64, P, P, I32, C.POINTER(P)]),
+    "gpm_graph_download": (I32, [P, P, P]),
     "gpm_graph_destroy": (I32, [P]),
     "gpm_graph_stats": (I32, [P, PI64, PI64, PI64, PI64]),
     "gpm_tri_count": (I32, [P, PU64]),

@@ -75,6 +75,19 @@ GPM_API int gpm_set_device(int32_t device);
 GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_t* col,
                              int32_t relabel, gpm_graph** out);
 
+/* Builds a graph on the GPU from m undirected edges (src[i], dst[i]) in host
+ * memory: symmetrises, drops self loops and duplicates, sorts and builds the
+ * offsets on the device — the host steps of DataLoader::general_load_data
+ * (reference src/dataloader.cpp:129-160) — then validates and (relabel != 0)
+ * relabels by degree like gpm_graph_create.  GPM_ERR_INVALID_ARG for an id
+ * outside [0, v_cnt) or 2m >= 2^32. */
+GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, const int32_t* dst,
+                                 int32_t relabel, gpm_graph** out);
+
+/* Copies the graph's CSR in the caller's ids (v_cnt + 1 offsets, e_cnt
+ * neighbours; sizes from gpm_graph_stats) to host arrays. */
+GPM_API int gpm_graph_download(const gpm_graph* g, uint32_t* rowptr, int32_t* col);
+
 /* Frees a graph (the reference's ~Graph, include/graph.h:24-27). */
 GPM_API int gpm_graph_destroy(gpm_graph* g);
 
@@ -258,6 +271,8 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
 
 /* Engine knobs (counts never depend on them):
  *   "warps_per_block", "blocks_per_sm", "chunk" (work-queue grab size),
+ *   "min_blocks" (1, or 3: the kernel variant for three blocks of at most
+ *   8 warps per SM),
  *   "split" (a loop at depth >= 2 with at least this many candidates is
  *   published so that idle warps take slices of it; 0 = off),
  *   "stage_max" (largest father set staged in shared memory),

@@ -164,7 +164,7 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
                     w->th[l].smem = shared[b].data();
                 }
                 auto body = [&](int) {
-                    match_kernel<false>(pairs.data(), n, cursors.data(), out.data(), scratch.data(), per_warp, k.chunk,
+                    match_kernel<false, 1>(pairs.data(), n, cursors.data(), out.data(), scratch.data(), per_warp, k.chunk,
                                         params, k.leaf, k.stage_cap, k.pair, k.pair ? tables.data() : nullptr, k.pair_log2, don,
                                         k.split, bm_words ? bitmaps.data() : nullptr, bm_words, k.bm_min,
                                         stats.data());

@@ -175,7 +175,8 @@ def test_engine_knobs_do_not_change_counts(engine, oracle):
     e = COUNTS["graphs"]["chung_lu_2k"]
     scheds = {k: gp.Schedule(_pattern(e["adj"][k]), 1, 1, True, g.v_cnt, g.e_cnt, e["tri_cnt"])
               for k in ("m4_2", "m5_3", "m5_20")}
-    for knobs in [{"chunk": 1}, {"warps_per_block": 4, "blocks_per_sm": 1}, {"chunk": 64, "warps_per_block": 16}]:
+    for knobs in [{"chunk": 1}, {"warps_per_block": 4, "blocks_per_sm": 1}, {"chunk": 64, "warps_per_block": 16},
+                  {"min_blocks": 3, "warps_per_block": 8}]:
         old = {k: gp.get_option(k) for k in knobs}
         for k, v in knobs.items():
             gp.set_option(k, v)
@@ -333,3 +334,23 @@ def test_leaf_bitmaps_match_oracle(engine, oracle):
     for opts in ({"bitmap_min": 1, "stage_max": 16}, {"bitmap_min": 1, "stage_max": 16, "split": 1},
                  {"bitmap_min": 0}):
         assert _with_options(opts, lambda: gp.batch_count(pairs, scheds)) == want, opts
+
+
+def test_gpu_csr_builder_matches_host(engine, oracle):
+    # edge list -> CSR on the GPU against the host builder: same offsets and
+    # neighbours (caller's ids), same counts; bad ids rejected
+    rng = np.random.default_rng(5)
+    for v, m in ((1, 0), (50, 400), (3000, 40000)):
+        src = rng.integers(0, v, m).astype(np.int32)
+        dst = rng.integers(0, v, m).astype(np.int32)
+        if m:
+            src[:5], dst[:5] = 0, 0  # self loops
+            src[5:9], dst[5:9] = src[9:13], dst[9:13]  # duplicates
+        h = gp.from_edges(v, src, dst)
+        d = gp.from_edges(v, src, dst, on_device=True)
+        assert np.array_equal(h.vertex, d.vertex) and np.array_equal(h.edge, d.edge)
+        if m:
+            s = gp.Schedule(gp.Pattern(gp.PatternType.House), 1, 1, True, d.v_cnt, d.e_cnt, oracle.triangles(d))
+            assert d.pattern_matching(s) == h.pattern_matching(s) == oracle.count(h, s)
+    with pytest.raises(gp.GpmError):
+        gp.from_edges(10, np.array([1, 2], np.int32), np.array([3, 10], np.int32), on_device=True)
