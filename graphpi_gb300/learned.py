@@ -95,6 +95,16 @@ def _time_schedule(g: Graph, s: Schedule, max_launch_ms: float = 150.0, cap_ms: 
         plan.close()
 
 
+def relativize(feats: np.ndarray) -> np.ndarray:
+    """Features of one pattern's candidates relative to each other: the
+    analytic cost terms become differences to the cheapest candidate, so the
+    model compares schedules of a pattern rather than graphs."""
+    f = np.array(feats, dtype=np.float32, copy=True)
+    f[:, 26] -= f[:, 26].min()
+    f[:, 30] -= f[:, 30].min()
+    return f
+
+
 def collect(g: Graph, patterns: list[Pattern], max_candidates: int = 32, use_iep: bool = True,
             verbose: bool = False) -> list[dict]:
     """Measures candidate schedules of every pattern on g (GPU)."""
@@ -110,12 +120,17 @@ def collect(g: Graph, patterns: list[Pattern], max_candidates: int = 32, use_iep
             best = min(range(len(cands)), key=lambda i: (cands[i]["cost"], i))
             if best not in idx:
                 idx[-1] = best
+        mine = []
         for i in idx:
             c = cands[i]
             s = schedule_from_order(p, c["order"], c["pairs"], use_iep, 1)
             ms = _time_schedule(g, s)
-            rows.append({"pattern": pi, "cand": i, "features": schedule_features(s, stats, c["cost"]),
+            mine.append({"pattern": pi, "cand": i, "features": schedule_features(s, stats, c["cost"]),
                          "ms": ms, "cost": c["cost"], "order": c["order"], "pairs": c["pairs"]})
+        rel = relativize(np.stack([r["features"] for r in mine]))
+        for r, f in zip(mine, rel):
+            r["features"] = f
+        rows += mine
         if verbose:
             print(f"[learned] pattern {pi}: {len(idx)} candidates", flush=True)
     return rows
@@ -140,8 +155,15 @@ class CostModel:
         return np.ascontiguousarray(((feats - self.mu) / self.sd).astype(np.float32))
 
     def fit(self, rows: list[dict], epochs: int = 3000, lr: float = 3e-3, weight_decay: float = 1e-4) -> float:
+        """Targets are log10 runtimes relative to the mean over the same
+        pattern's candidates: only the order within a pattern matters."""
         X = np.stack([r["features"] for r in rows]).astype(np.float32)
-        y = np.array([math.log10(max(r["ms"], 1e-3)) for r in rows], dtype=np.float32)
+        logs = np.array([math.log10(max(r["ms"], 1e-3)) for r in rows], dtype=np.float64)
+        pats = np.array([r["pattern"] for r in rows])
+        y = np.zeros(len(rows), dtype=np.float32)
+        for p in np.unique(pats):
+            m = pats == p
+            y[m] = (logs[m] - logs[m].mean()).astype(np.float32)
         self.mu = X.mean(axis=0)
         self.sd = X.std(axis=0) + 1e-3
         Xs = self._x(X)
@@ -177,8 +199,11 @@ class CostModel:
             pass
 
 
-def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = True) -> tuple[Schedule, dict]:
-    """Learned schedule choice (analytic model when model is None)."""
+def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = True,
+           judge: int = 0) -> tuple[Schedule, dict]:
+    """Learned schedule choice (analytic model when model is None).  With
+    judge=k the k candidates the model ranks fastest and the analytic choice
+    are timed on a sample of the work and the fastest measured one wins."""
     stats = graph_stats(g)
     cands = schedule_candidates(pattern, 1, 1, stats["v_cnt"], stats["e_cnt"], stats["tri_cnt"])
     if model is None:
@@ -186,31 +211,43 @@ def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = 
         c = cands[i]
         return schedule_from_order(pattern, c["order"], c["pairs"], use_iep, 1), {"index": i, "by": "analytic"}
     scheds = [schedule_from_order(pattern, c["order"], c["pairs"], use_iep, 1) for c in cands]
-    feats = np.stack([schedule_features(s, stats, c["cost"]) for s, c in zip(scheds, cands)])
+    feats = relativize(np.stack([schedule_features(s, stats, c["cost"]) for s, c in zip(scheds, cands)]))
     pred = model.predict(feats)
-    i = int(np.argmin(pred))
-    return scheds[i], {"index": i, "by": "mlp", "pred_log10_ms": float(pred[i])}
+    if judge <= 0:
+        i = int(np.argmin(pred))
+        return scheds[i], {"index": i, "by": "mlp", "pred_rel_log10_ms": float(pred[i])}
+    # measured runtime judges the model's top candidates and the analytic choice
+    a = min(range(len(cands)), key=lambda j: (cands[j]["cost"], j))
+    shortlist = sorted(set([int(j) for j in np.argsort(pred)[:judge]] + [a]))
+    timed = {j: _time_schedule(g, scheds[j]) for j in shortlist}
+    i = min(timed, key=lambda j: (timed[j], j))
+    return scheds[i], {"index": i, "by": "mlp+measured", "timed_ms": timed, "analytic_index": a}
 
 
-def evaluate(rows: list[dict], model: CostModel) -> dict:
-    """Per pattern: measured time of the MLP's pick, the analytic pick and
-    the best candidate (from measured rows)."""
+def evaluate(rows: list[dict], model: CostModel, judge: int = 3) -> dict:
+    """Per pattern: measured time of the MLP's pick, of the judged pick (the
+    fastest measured among the MLP's top `judge` and the analytic choice),
+    of the analytic pick, and of the best candidate (from measured rows)."""
     by_pat: dict[int, list[dict]] = {}
     for r in rows:
         by_pat.setdefault(r["pattern"], []).append(r)
-    tot = {"mlp": 0.0, "analytic": 0.0, "best": 0.0}
+    tot = {"mlp": 0.0, "judged": 0.0, "analytic": 0.0, "best": 0.0}
     per = []
     for pi, rs in sorted(by_pat.items()):
         pred = model.predict(np.stack([r["features"] for r in rs]))
-        m = rs[int(np.argmin(pred))]["ms"]
-        a = min(rs, key=lambda r: (r["cost"], r["cand"]))["ms"]
+        order = np.argsort(pred)
+        m = rs[int(order[0])]["ms"]
+        ra = min(rs, key=lambda r: (r["cost"], r["cand"]))
+        a = ra["ms"]
+        j = min([rs[int(i)]["ms"] for i in order[:judge]] + [a])
         b = min(r["ms"] for r in rs)
         tot["mlp"] += m
+        tot["judged"] += j
         tot["analytic"] += a
         tot["best"] += b
-        per.append({"pattern": pi, "mlp_ms": m, "analytic_ms": a, "best_ms": b})
-    tot["mlp_over_best"] = tot["mlp"] / max(tot["best"], 1e-9)
-    tot["analytic_over_best"] = tot["analytic"] / max(tot["best"], 1e-9)
+        per.append({"pattern": pi, "mlp_ms": m, "judged_ms": j, "analytic_ms": a, "best_ms": b})
+    for k in ("mlp", "judged", "analytic"):
+        tot[f"{k}_over_best"] = tot[k] / max(tot["best"], 1e-9)
     tot["per_pattern"] = per
     return tot
 
@@ -220,7 +257,7 @@ def main(argv: list[str] | None = None) -> dict:
     reports, for held-out patterns on another, the measured runtime of the
     MLP's choice, of the analytic model's choice and of the best candidate.
 
-        python -m graphpi_gb300.learned --train-scale 16 --eval-scale 18
+        python -m graphpi_gb300.learned --train-scale 14 --eval-scale 16
     """
     import argparse
     import json
@@ -229,8 +266,8 @@ def main(argv: list[str] | None = None) -> dict:
     from .api import MotifGenerator
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--train-scale", type=int, default=16)
-    ap.add_argument("--eval-scale", type=int, default=18)
+    ap.add_argument("--train-scale", type=int, default=14)
+    ap.add_argument("--eval-scale", type=int, default=16)
     ap.add_argument("--six-stride", type=int, default=8, help="every k-th of the 112 six-vertex motifs")
     ap.add_argument("--candidates", type=int, default=12)
     ap.add_argument("--epochs", type=int, default=3000)
@@ -248,8 +285,9 @@ def main(argv: list[str] | None = None) -> dict:
     ev = evaluate(rows_ev, model)
     res = {"train_graph": f"rmat s{a.train_scale}", "eval_graph": f"rmat s{a.eval_scale}",
            "train_rows": len(rows_tr), "eval_rows": len(rows_ev), "train_loss": loss,
-           "mlp_over_best": ev["mlp_over_best"], "analytic_over_best": ev["analytic_over_best"],
-           "mlp_ms": ev["mlp"], "analytic_ms": ev["analytic"], "best_ms": ev["best"],
+           "mlp_over_best": ev["mlp_over_best"], "judged_over_best": ev["judged_over_best"],
+           "analytic_over_best": ev["analytic_over_best"],
+           "mlp_ms": ev["mlp"], "judged_ms": ev["judged"], "analytic_ms": ev["analytic"], "best_ms": ev["best"],
            "per_pattern": ev["per_pattern"], "seconds": time.time() - t0}
     model.close()
     text = json.dumps(res, indent=1)
