@@ -228,6 +228,14 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     k0 = kernel_ms[0]
     achieved = algo_bytes / (k0 / 1e3) / 1e9
     peak, peak_kind = _peak_hbm()
+    # DRAM bytes of one batched launch from the committed one-pass ncu capture
+    traffic, traffic_src = None, None
+    cap = ROOT / "profiles" / "match_kernel_dram.json"
+    if args.scale == 22 and cap.exists():
+        c = json.loads(cap.read_text())
+        traffic = c.get("dram_bytes_per_launch")
+        traffic_src = f"ncu capture of stripe {c.get('stripe')} of {c.get('stripes')}, {c.get('knobs')}"
+
 
     # ---- e2e through the host-buffer C ABI ---------------------------------
     vtx = torch.from_numpy(g.vertex.view(np.int32)).pin_memory()
@@ -290,8 +298,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                 "d2h_bytes_per_step": 16 * n, "ms_per_step": e2e_ms / args.steps},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                     "algo_bytes_per_launch": algo_bytes},
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
+                     "peak_kind": peak_kind, "algo_bytes_per_launch": algo_bytes},
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
     }

@@ -428,7 +428,16 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         ls.blocks = (ls.blocks + 1) / 2;
     const int alpha4[3] = {(int)o.merge_alpha4[0], (int)o.merge_alpha4[1], (int)o.merge_alpha4[2]};
     GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, c->stream));
-    ls.chunk = (int)o.chunk;
+    // A grab takes `chunk` tasks of the stripe, but never leaves warps
+    // without a task: when a stripe holds fewer than chunk tasks per warp
+    // (thin benchmark stripes), grabs shrink down to one task.
+    {
+        const unsigned long long warps = (unsigned long long)ls.blocks * ls.wpb;
+        const unsigned long long stripes = (unsigned long long)std::max<int64_t>(1, o.stripes);
+        unsigned long long fewest = ~0ull;
+        for (const PairDesc& d : ls.descs) fewest = std::min(fewest, (d.ntasks + stripes - 1) / stripes);
+        ls.chunk = (int)std::max<unsigned long long>(1, std::min<unsigned long long>(o.chunk, fewest / warps));
+    }
     ls.leaf_on = (int)o.leaf_batch;
     ls.pair_on = 0;
     if (o.pair_leaf) {

@@ -98,7 +98,7 @@ __device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned en
 
 // Takes the next slice of record r (generation gen); lo == hi when the loop
 // is exhausted or the slot holds another generation.  A slice is 1/32 of
-// what is left, within [1, 64] candidates of a loop or [32, 1024] of a
+// what is left, within [1, 64] candidates of a loop or [8, 128] of a
 // batched leaf level.  Lock-free: a failed compare-and-swap means another
 // warp took a slice, so the retries are bounded by the loop length (< 2^24).
 __device__ void don_claim(Donation* r, unsigned gen, bool leaf, int& lo, int& hi) {
@@ -109,7 +109,7 @@ __device__ void don_claim(Donation* r, unsigned gen, bool leaf, int& lo, int& hi
         const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
         if (next >= end) return;
         const unsigned want = (end - next) >> 5;
-        const unsigned take = min(end - next, leaf ? min(1024u, max(32u, want)) : min(64u, max(1u, want)));
+        const unsigned take = min(end - next, leaf ? min(128u, max(8u, want)) : min(64u, max(1u, want)));
         const unsigned long long got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
         if (got == w) {
             lo = (int)next;
