@@ -357,7 +357,7 @@ def run_reference(args, rank: int, world: int) -> dict | None:
         "metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int64/int128 counts", "data": "synthetic (seeded R-MAT generator)",
-        "config": {"workload": "rmat_s22 x 29 motifs (3-5 vertices)", "step": "bounded root sample per step"},
+        "config": {"workload": f"rmat_s{args.scale} x 29 motifs (3-5 vertices)", "step": "bounded root sample per step"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "embeddings/s", "cores": threads, "kind": "port",
                          "sample": samples[0]},
