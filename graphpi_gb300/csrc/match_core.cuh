@@ -290,7 +290,7 @@ __device__ __forceinline__ unsigned pair_slot(int x, unsigned mask) { return ((u
 __device__ bool pair_add(unsigned long long* T, unsigned mask, unsigned epoch, int x) {
     unsigned slot = pair_slot(x, mask);
     for (unsigned probes = 0; probes <= mask; ++probes) {
-        unsigned long long old = T[slot];
+        unsigned long long old = __ldcg(&T[slot]);
         for (;;) {
             const bool live = (unsigned)(old >> 48) == (epoch & 0xffffu);
             if (live && (int)((old >> 24) & 0xffffff) == x) {
@@ -315,7 +315,7 @@ __device__ bool pair_add(unsigned long long* T, unsigned mask, unsigned epoch, i
 __device__ unsigned pair_get(const unsigned long long* T, unsigned mask, unsigned epoch, int x) {
     unsigned slot = pair_slot(x, mask);
     for (unsigned probes = 0; probes <= mask; ++probes) {
-        const unsigned long long w = T[slot];
+        const unsigned long long w = __ldcg(&T[slot]);  // written by L2 atomics: skip L1
         if ((unsigned)(w >> 48) != (epoch & 0xffffu)) return 0;
         if ((int)((w >> 24) & 0xffffff) == x) return (unsigned)(w & 0xffffff);
         slot = (slot + 1) & mask;
@@ -345,6 +345,10 @@ struct WarpCtx {
     unsigned pmask;
     DonationArea* don;         // null: no donation
     int split_min;             // smallest loop that is donated
+    unsigned* dense;           // pool of per-vertex counter arrays for big pair sums (null: none)
+    unsigned* dense_lock;      // one try-lock word per array
+    int dense_slots;
+    int dense_words;           // counters per array (>= v_cnt of every graph)
     unsigned* bm;              // this warp's two bitmaps over vertex ids (null: none)
     int bm_words;              // words per bitmap
     int bm_min;                // smallest fixed set tested through a bitmap
@@ -354,8 +358,9 @@ struct WarpCtx {
 
     // Bitmap variant of a membership test: marks set S[0, n) in bitmap r.
     // Used for fixed sets too large for shared memory when the elements to
-    // test outnumber an eighth of the set: one load per test instead of a
-    // binary search of log2(n) dependent loads.  bitmap_clear undoes it.
+    // test outnumber the set twice over, so the two passes over the set
+    // (mark, clear) are paid back: one load per test instead of a binary
+    // search of log2(n) dependent loads.  bitmap_clear undoes it.
     __device__ const unsigned* bitmap_set(const int* S, int n, int r) {
         unsigned* b = bm + (size_t)r * bm_words;
         for (int i = lane; i < n; i += 32) {
@@ -372,7 +377,7 @@ struct WarpCtx {
         __syncwarp();
     }
     __device__ __forceinline__ bool use_bitmap(int n, long long tests) const {
-        return bm != nullptr && bm_min > 0 && n > stage_cap && n >= bm_min && tests * 8 >= n;
+        return bm != nullptr && bm_min > 0 && n > stage_cap && n >= bm_min && tests >= 2ll * n;
     }
 
     // copies a fixed set into shared-memory region r when it fits
@@ -414,6 +419,103 @@ struct WarpCtx {
         return hit;
     }
 
+    // c term of a pair sum: v in both candidate lists pairs with itself,
+    // contributing |N(v) ∩ [0, bnd) \ chosen| (this lane's share)
+    __device__ long long pair_c_term(const int* candA, int na, const int* candB, int nb, int bnd, int L1) {
+        long long sum = 0;
+        for (int base = 0; base < na; base += 32) {
+            const int j = base + lane;
+            if (j < na) {
+                const int v = candA[j];
+                if (!chosen_before(v, L1) && contains(candB, nb, v)) {
+                    const unsigned st = g.rowptr[v];
+                    const int* nv = g.col + st;
+                    const int len = lower_bound_u(nv, (int)(g.rowptr[v + 1] - st), bnd);
+                    int in = 0;
+                    for (int q = 0; q < L1; ++q) in += contains(nv, len, s->chosen[q]) ? 1 : 0;
+                    sum += (long long)(len - in);
+                }
+            }
+        }
+        return sum;
+    }
+
+    // Neighbour lists of cand[0, n) below bnd, for each element x not chosen
+    // before depth L1: op 0 adds one to cnt[x], op 1 sums cnt[x], op 2 zeroes it.
+    __device__ long long dense_pass(const int* cand, int n, int bnd, int L1, unsigned* cnt, int op) {
+        long long sum = 0;
+        for (int base = 0; base < n; base += 32) {
+            const int j = base + lane;
+            unsigned st = 0;
+            int len = 0;
+            if (j < n) {
+                const int v = cand[j];
+                if (!chosen_before(v, L1)) {
+                    st = g.rowptr[v];
+                    len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
+                    if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
+                }
+            }
+            int pre;
+            const int M = warp_scan(len, pre);
+            for (int eb = 0; eb < M; eb += 32) {
+                const int e = eb + lane;
+                const int c = owner(pre, e);
+                const unsigned stc = __shfl_sync(kFull, st, c);
+                const int prc = __shfl_sync(kFull, pre, c);
+                if (e < M) {
+                    const int x = g.col[stc + (e - prc)];
+                    if (!chosen_before(x, L1)) {
+                        if (op == 0) atomicAdd(&cnt[x], 1u);
+                        else if (op == 1) sum += __ldcg(&cnt[x]);
+                        else cnt[x] = 0u;
+                    }
+                }
+            }
+        }
+        return sum;
+    }
+
+    // The pair sum of pair_level with a dense counter array from the pool
+    // when its hash table is too small: O(mA + 2 mB) direct-indexed updates
+    // instead of |A| loops over B's lists.  Returns false (nothing done) when
+    // the work would be too long for one warp or no array is free; the lock
+    // is a try-lock, so no warp waits.
+    __device__ bool pair_level_dense(const int* candA, int na, const int* candB, int nb, int bnd, bool a_fills,
+                                     long long ops, __int128& out) {
+        constexpr long long kDenseMaxOps = 1ll << 24;
+        if (!dense || ops > kDenseMaxOps || g.v_cnt > dense_words) return false;
+        int slot = -1;
+        if (lane == 0) {
+            for (int i = 0; i < dense_slots && slot < 0; ++i) {
+                const int k = (int)((gw + i) % dense_slots);
+                if (atomicCAS(&dense_lock[k], 0u, 1u) == 0u) slot = k;
+            }
+        }
+        slot = __shfl_sync(kFull, slot, 0);
+        if (slot < 0) return false;
+        unsigned* cnt = dense + (size_t)slot * (size_t)dense_words;
+        const int L1 = P->L - 1;
+        const int* fill = a_fills ? candA : candB;
+        const int nfill = a_fills ? na : nb;
+        const int* probe = a_fills ? candB : candA;
+        const int nprobe = a_fills ? nb : na;
+        dense_pass(fill, nfill, bnd, L1, cnt, 0);
+        __threadfence();
+        __syncwarp();
+        long long sum = dense_pass(probe, nprobe, bnd, L1, cnt, 1);
+        __syncwarp();
+        dense_pass(fill, nfill, bnd, L1, cnt, 2);
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) atomicExch(&dense_lock[slot], 0u);
+        sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+        out = lane == 0 ? (__int128)sum : (__int128)0;
+        return true;
+    }
+
     // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
     // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
     // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
@@ -451,8 +553,8 @@ struct WarpCtx {
             (side == 0 ? ma : mb) = m;
         }
         const long long mins = min(ma, mb);
-        if (mins * 2 > (long long)pmask + 1) return false;
         const bool a_fills = ma < mb;
+        if (mins * 2 > (long long)pmask + 1) return pair_level_dense(candA, na, candB, nb, bnd, a_fills, ma + mb + mins, out);
         __syncwarp();
         if (lane == 0) {
             s->epoch = (s->epoch + 1) & 0xffffu;
@@ -503,21 +605,7 @@ struct WarpCtx {
                 __syncwarp();
             }
         }
-        // c term: v in both candidate lists pairs with itself
-        for (int base = 0; base < na; base += 32) {
-            const int j = base + lane;
-            if (j < na) {
-                const int v = candA[j];
-                if (!chosen_before(v, L1) && contains(candB, nb, v)) {
-                    const unsigned st = g.rowptr[v];
-                    const int* nv = g.col + st;
-                    const int len = lower_bound_u(nv, (int)(g.rowptr[v + 1] - st), bnd);
-                    int in = 0;
-                    for (int q = 0; q < L1; ++q) in += contains(nv, len, s->chosen[q]) ? 1 : 0;
-                    sum -= (long long)(len - in);
-                }
-            }
-        }
+        sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
 #pragma unroll
         for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
         out = lane == 0 ? (__int128)sum : (__int128)0;
@@ -1151,7 +1239,8 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match
                                                     int leaf_on, int stage_cap, int pair_on,
                                                     unsigned long long* __restrict__ pair_tables, int pair_log2,
                                                     DonationArea* don, int split_min, unsigned* bitmaps,
-                                                    int bm_words, int bm_min,
+                                                    int bm_words, int bm_min, unsigned* dense_pool,
+                                                    int dense_slots, int dense_words,
                                                     unsigned long long* __restrict__ stats) {
     // params[0] = stripes, params[1] = stripe (device memory, so a captured
     // graph can replay with new values)
@@ -1179,6 +1268,10 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match
     w.don = don;
     w.split_min = split_min;
     w.gw = gw;
+    w.dense_slots = dense_pool ? dense_slots : 0;
+    w.dense_words = dense_words;
+    w.dense_lock = dense_pool;  // dense_slots lock words, then 64-word aligned arrays
+    w.dense = dense_pool ? dense_pool + ((dense_slots + 63) & ~63) : nullptr;
     w.bm = bitmaps ? bitmaps + (size_t)gw * 2 * (size_t)bm_words : nullptr;
     w.bm_words = bm_words;
     w.bm_min = bm_min;
