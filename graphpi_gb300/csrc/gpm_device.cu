@@ -365,6 +365,8 @@ struct LaunchSetup {
     int bm_words = 0;  // words per leaf bitmap (0: no bitmaps)
     int bm_min = 0;
     int min_blocks = 1;  // kernel variant: 1 or 3 resident blocks per SM
+    int dense_slots = 0;  // pool of per-vertex counter arrays for big pair sums
+    int dense_words = 0;
     bool count_bytes = false;
 };
 
@@ -455,6 +457,13 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
             ls.pair_log2 = kPairLog2Max;
             while (ls.pair_log2 > kPairLog2Min && warps * ((size_t)8 << ls.pair_log2) > room) --ls.pair_log2;
         }
+        // dense counter arrays for the pair sums too big for a table: up to
+        // 64, within an eighth of the free memory
+        int vmax = 0;
+        for (int i = 0; i < n; ++i) vmax = std::max(vmax, graphs[i]->v_cnt);
+        ls.dense_words = vmax;
+        ls.dense_slots = (int)std::min<int64_t>(o.dense_slots, (int64_t)(room / 2 / ((size_t)vmax * 4 + 1)));
+        if (ls.dense_slots < 1) ls.dense_slots = 0;
     }
     ls.split_min = (int)o.split;
     // two bitmaps over vertex ids per warp for the batched leaves
@@ -480,8 +489,15 @@ static size_t small_words(int n) { return (size_t)n * 3 + 4; }
 // Scratch of a launch: per-warp set slots, per-warp pair tables, then the
 // donation records (zeroed before every launch).
 struct ScratchLayout {
-    size_t tables = 0, donation = 0, bitmaps = 0, total = 0;
+    size_t tables = 0, donation = 0, bitmaps = 0, dense = 0, total = 0;
 };
+
+// lock words padded to 64, then dense_slots arrays of dense_words counters
+static size_t dense_bytes(const LaunchSetup& ls) {
+    if (!ls.dense_slots) return 0;
+    return (((size_t)ls.dense_slots + 63) & ~(size_t)63) * sizeof(unsigned) +
+           (size_t)ls.dense_slots * ls.dense_words * sizeof(unsigned);
+}
 
 static size_t bitmap_bytes(const LaunchSetup& ls) {
     return (size_t)ls.blocks * ls.wpb * 2 * (size_t)ls.bm_words * sizeof(unsigned);
@@ -499,6 +515,9 @@ static ScratchLayout scratch_layout(const LaunchSetup& ls) {
     b = (b + 255) & ~(size_t)255;
     s.bitmaps = b;
     b += bitmap_bytes(ls);
+    b = (b + 255) & ~(size_t)255;
+    s.dense = b;
+    b += dense_bytes(ls);
     s.total = std::max<size_t>(b, 1);
     return s;
 }
@@ -523,9 +542,14 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
         const cudaError_t e = cudaMemsetAsync(bitmaps, 0, bitmap_bytes(ls), st);
         if (e != cudaSuccess) return e;
     }
+    unsigned* dense = ls.dense_slots ? (unsigned*)((char*)scratch + lay.dense) : nullptr;
+    if (dense) {
+        const cudaError_t e = cudaMemsetAsync(dense, 0, dense_bytes(ls), st);
+        if (e != cudaSuccess) return e;
+    }
 #define GPM_MATCH_ARGS                                                                                        \
     d_pairs, n, cursors, out, scratch, ls.per_warp, ls.chunk, params, ls.leaf_on, ls.stage_cap, ls.pair_on, tables, \
-        ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, stats
+        ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, dense, ls.dense_slots, ls.dense_words, stats
     if (ls.count_bytes)
         match_kernel<true, 1><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
     else if (ls.min_blocks == 3)
@@ -1189,7 +1213,7 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     GPM_CK(cudaFuncSetAttribute(match_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     match_kernel<false, 1><<<(unsigned)(warps / wpb), wpb * 32, smem, st>>>(
         d_pair, 1, ctrl, ctrl + 1, warp_scratch, per_warp, (int)o.chunk, ctrl + 5, (int)o.leaf_batch, stage_cap,
-        0, nullptr, 0, nullptr, 0, nullptr, 0, 0, ctrl + 3);
+        0, nullptr, 0, nullptr, 0, nullptr, 0, 0, nullptr, 0, 0, ctrl + 3);
     GPM_CK(cudaGetLastError());
     unsigned long long raw[2] = {0, 0};
     GPM_CK(cudaMemcpyAsync(raw, ctrl + 1, sizeof raw, cudaMemcpyDeviceToHost, st));

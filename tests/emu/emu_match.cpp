@@ -111,6 +111,7 @@ std::vector<Sched> motif_schedules(const Csr& g, int k, bool iep, int stride) {
 struct Knobs {
     int blocks = 2, wpb = 4, chunk = 2, stage_cap = 64, leaf = 1, pair = 0, split = 0, pair_log2 = 13;
     int bm_min = 0;  // > 0: leaf bitmaps for fixed sets of at least this size
+    int dense = 0;   // > 0: that many dense counter arrays for big pair sums
     unsigned long long stripes = 1, stripe = 0;
 };
 
@@ -145,6 +146,8 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     std::vector<unsigned long long> tables;
     if (k.pair) tables.assign((size_t)warps << k.pair_log2, 0ull);
     const int bm_words = k.bm_min > 0 ? (g.v + 31) / 32 : 0;
+    // dense pool: lock words padded to 64, then k.dense arrays of g.v counters
+    std::vector<unsigned> dense(k.dense ? 64 + (size_t)k.dense * g.v : 0, 0u);
     std::vector<unsigned> bitmaps((size_t)warps * 2 * bm_words, 0u);
     DonationArea* don = k.split > 0 ? new DonationArea() : nullptr;
     if (don) std::memset((void*)don, 0, sizeof(DonationArea));
@@ -167,7 +170,7 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
                     match_kernel<false, 1>(pairs.data(), n, cursors.data(), out.data(), scratch.data(), per_warp, k.chunk,
                                         params, k.leaf, k.stage_cap, k.pair, k.pair ? tables.data() : nullptr, k.pair_log2, don,
                                         k.split, bm_words ? bitmaps.data() : nullptr, bm_words, k.bm_min,
-                                        stats.data());
+                                        k.dense ? dense.data() : nullptr, k.dense, g.v, stats.data());
                 };
                 gpm_emu::run_warp(*w, body);
                 delete w;
@@ -193,6 +196,12 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     for (unsigned w : bitmaps)
         if (w) {
             std::printf("bitmap left dirty after the launch\n");
+            ++failures;
+            break;
+        }
+    for (unsigned w : dense)
+        if (w) {
+            std::printf("dense counters or locks left dirty after the launch\n");
             ++failures;
             break;
         }
@@ -289,11 +298,14 @@ void case_pair() {
     }
     for (int split : {0, 1})
         for (int log2 : {13, 5}) {  // a table that holds every task, and one that forces the fallback
-            Knobs k;
-            k.pair = 1;
-            k.split = split;
-            k.pair_log2 = log2;
-            expect_oracle("pair-sum", g, ss, k);
+            for (int dense : {0, 2}) {  // the fallback: loops, or dense counter arrays
+                Knobs k;
+                k.pair = 1;
+                k.split = split;
+                k.pair_log2 = log2;
+                k.dense = dense;
+                expect_oracle("pair-sum", g, ss, k);
+            }
         }
 }
 

@@ -272,6 +272,8 @@ inline int __ffs(int x) { return __builtin_ffs(x); }
 inline int __clz(int x) { return x == 0 ? 32 : __builtin_clz((unsigned)x); }
 
 inline void __threadfence() { __atomic_thread_fence(__ATOMIC_SEQ_CST); }
+template <class T>
+inline T __ldcg(const T* p) { return __atomic_load_n(p, __ATOMIC_RELAXED); }
 inline void __nanosleep(unsigned) { std::this_thread::yield(); }
 
 template <class T>

@@ -303,10 +303,12 @@ def test_pair_sum_leaf_matches_oracle(engine, oracle):
         assert scheds, "no plan takes the pair-sum leaf"
         want = [oracle.count(g, s) for s in scheds]
         for split in (0, 1):
-            for log2 in (0, 6):  # tables sized to memory, and tiny ones that force the fallback
-                opts = {"pair_leaf": 1, "split": split, "pair_log2": log2}
+            # tables sized to memory; tiny ones that send tasks to the dense
+            # counter arrays; tiny ones without arrays (the loops)
+            for log2, dense in ((0, 64), (6, 64), (6, 0)):
+                opts = {"pair_leaf": 1, "split": split, "pair_log2": log2, "dense_slots": dense}
                 got = _with_options(opts, lambda: gp.batch_count([g] * len(scheds), scheds))
-                assert got == want, (split, log2)
+                assert got == want, (split, log2, dense)
         assert _with_options({"pair_leaf": 0}, lambda: gp.batch_count([g] * len(scheds), scheds)) == want
 
 
