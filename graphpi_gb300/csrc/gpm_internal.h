@@ -21,9 +21,9 @@ struct Options {
     int64_t count_bytes = 0;    // 1: count algorithmic bytes
     int64_t timeout_ms = 2000;  // bounded device waits
     int64_t stage_max = 1024;   // largest fixed set staged in shared memory (ints)
-    int64_t leaf_batch = 1;     // 1: batched deepest level where the plan allows
+    int64_t leaf_batch = 0;     // 1: batched deepest level where the plan allows
     int64_t pair_leaf = 1;      // 1: pair sums over the last two levels where the plan allows
-    int64_t dense_slots = 64;   // dense counter arrays for pair sums too big for a table (0 = none)
+    int64_t dense_slots = 0;    // dense counter arrays for pair sums too big for a table (0 = none)
     int64_t pair_log2 = 0;      // log2 entries of each warp's pair-sum table (0: sized to free memory)
     int64_t min_blocks = 1;     // 3: the kernel variant built for three 8-warp blocks per SM
     int64_t bitmap_min = 4096;  // fixed leaf sets this large are tested through a bitmap; 0 = never

@@ -277,10 +277,10 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
  *   published so that idle warps take slices of it; 0 = off),
  *   "stage_max" (largest father set staged in shared memory),
  *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan allows;
- *   both on by default), "pair_log2" (entries per warp of the pair-sum
+ *   the pair-sum leaf is on by default, the batched leaf off), "pair_log2" (entries per warp of the pair-sum
  *   table as a power of two; 0 = sized to free memory), "dense_slots"
  *   (per-vertex counter arrays shared by pair sums too big for the table;
- *   0 = none), "bitmap_min"
+ *   default 0 = none), "bitmap_min"
  *   (fixed leaf sets at least this large are tested through a per-warp
  *   bitmap instead of a binary search; 0 = never),
  *   "merge_alpha4_small"/"_mid"/"_large" (merge vs search per length bucket),

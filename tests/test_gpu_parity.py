@@ -220,20 +220,12 @@ def test_leaf_batch_matches_per_candidate_path(engine, oracle):
     for flags in [(1, 1, True), (1, 1, False), (0, 1, True)]:
         scheds = [gp.Schedule(p, flags[0], flags[1], flags[2], g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
         scheds = [s for s in scheds if s.is_pattern_valid]
-        batched = gp.batch_count([g] * len(scheds), scheds)
-        gp.set_option("leaf_batch", 0)
-        try:
-            plain = gp.batch_count([g] * len(scheds), scheds)
-        finally:
-            gp.set_option("leaf_batch", 1)
+        pairs = [g] * len(scheds)
+        batched = _with_options({"leaf_batch": 1}, lambda: gp.batch_count(pairs, scheds))
+        plain = _with_options({"leaf_batch": 0}, lambda: gp.batch_count(pairs, scheds))
         assert batched == plain == [oracle.count(g, s) for s in scheds]
     # tiny staging area forces the global-memory probe path
-    old = gp.get_option("stage_max")
-    gp.set_option("stage_max", 16)
-    try:
-        assert gp.batch_count([g] * len(scheds), scheds) == batched
-    finally:
-        gp.set_option("stage_max", old)
+    assert _with_options({"leaf_batch": 1, "stage_max": 16}, lambda: gp.batch_count(pairs, scheds)) == batched
 
 
 def test_uneven_multi_graph_batch(engine, oracle):
@@ -333,8 +325,9 @@ def test_leaf_bitmaps_match_oracle(engine, oracle):
     scheds += [gp.Schedule(p, 1, 1, False, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()[9::5]]
     want = [oracle.count(g, s) for s in scheds]
     pairs = [g] * len(scheds)
-    for opts in ({"bitmap_min": 1, "stage_max": 16}, {"bitmap_min": 1, "stage_max": 16, "split": 1},
-                 {"bitmap_min": 0}):
+    for opts in ({"leaf_batch": 1, "bitmap_min": 1, "stage_max": 16},
+                 {"leaf_batch": 1, "bitmap_min": 1, "stage_max": 16, "split": 1},
+                 {"leaf_batch": 1, "bitmap_min": 0}):
         assert _with_options(opts, lambda: gp.batch_count(pairs, scheds)) == want, opts
 
 
