@@ -142,6 +142,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     gp.set_option("pair_log2", args.pair_log2)
     if args.leaf_batch is not None:
         gp.set_option("leaf_batch", args.leaf_batch)
+    if args.pair_max_ops is not None:
+        gp.set_option("pair_max_ops", args.pair_max_ops)
 
     def batched(stripe: int) -> list[int]:
         gp.set_option("stripe", stripe)
@@ -379,6 +381,8 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark graph)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-tuning", action="store_true", help="ignore the stored autotuner table")
+    ap.add_argument("--pair-max-ops", type=int, default=None,
+                    help="longest pair sum one warp takes on (default: the engine's)")
     ap.add_argument("--leaf-batch", type=int, default=None, choices=[0, 1],
                     help="force the batched deepest level on or off (default: the engine's)")
     ap.add_argument("--pair-log2", type=int, default=0,

@@ -687,6 +687,7 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "pair_leaf") slot = &o.pair_leaf, lo = 0, hi = 1;
     else if (k == "pair_log2") slot = &o.pair_log2, lo = 0, hi = 24;
     else if (k == "dense_slots") slot = &o.dense_slots, lo = 0, hi = 1024;
+    else if (k == "pair_max_ops") slot = &o.pair_max_ops, lo = 0, hi = (int64_t)1 << 40;
     else if (k == "bitmap_min") slot = &o.bitmap_min, lo = 0, hi = 1 << 30;
     else if (k == "min_blocks") {
         if (value != 1 && value != 3) {
@@ -729,6 +730,7 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "pair_leaf") *value = o.pair_leaf;
     else if (k == "pair_log2") *value = o.pair_log2;
     else if (k == "dense_slots") *value = o.dense_slots;
+    else if (k == "pair_max_ops") *value = o.pair_max_ops;
     else if (k == "bitmap_min") *value = o.bitmap_min;
     else if (k == "min_blocks") *value = o.min_blocks;
     else if (k == "split") *value = o.split;

@@ -24,6 +24,7 @@ struct Options {
     int64_t leaf_batch = 0;     // 1: batched deepest level where the plan allows
     int64_t pair_leaf = 1;      // 1: pair sums over the last two levels where the plan allows
     int64_t dense_slots = 0;    // dense counter arrays for pair sums too big for a table (0 = none)
+    int64_t pair_max_ops = 0;   // longest pair sum one warp takes on (0: no cap)
     int64_t pair_log2 = 0;      // log2 entries of each warp's pair-sum table (0: sized to free memory)
     int64_t min_blocks = 1;     // 3: the kernel variant built for three 8-warp blocks per SM
     int64_t bitmap_min = 4096;  // fixed leaf sets this large are tested through a bitmap; 0 = never

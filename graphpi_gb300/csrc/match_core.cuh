@@ -193,6 +193,10 @@ __device__ int warp_merge(const int* A, int na, const int* B, int nb, int* out, 
 // list's length (< 256, < 8192, larger); the autotuner sets them.
 __constant__ int c_merge_alpha4[3] = {4, 4, 4};
 
+// Longest pair sum (elements of both sides' lists) one warp takes on; a
+// longer one runs as loops, which donation spreads over idle warps (0: no cap).
+__constant__ long long c_pair_max_ops = 0;
+
 __device__ __forceinline__ bool prefer_merge(int na, int nb) {
     const int lg = 32 - __clz(nb | 1);
     const int a4 = c_merge_alpha4[nb < 256 ? 0 : (nb < 8192 ? 1 : 2)];
@@ -552,6 +556,7 @@ struct WarpCtx {
             }
             (side == 0 ? ma : mb) = m;
         }
+        if (c_pair_max_ops > 0 && ma + mb > c_pair_max_ops) return false;
         const long long mins = min(ma, mb);
         const bool a_fills = ma < mb;
         if (mins * 2 > (long long)pmask + 1) return pair_level_dense(candA, na, candB, nb, bnd, a_fills, ma + mb + mins, out);

@@ -297,10 +297,10 @@ def test_pair_sum_leaf_matches_oracle(engine, oracle):
         for split in (0, 1):
             # tables sized to memory; tiny ones that send tasks to the dense
             # counter arrays; tiny ones without arrays (the loops)
-            for log2, dense in ((0, 64), (6, 64), (6, 0)):
-                opts = {"pair_leaf": 1, "split": split, "pair_log2": log2, "dense_slots": dense}
+            for log2, dense, cap in ((0, 64, 0), (6, 64, 0), (6, 0, 0), (0, 0, 64)):
+                opts = {"pair_leaf": 1, "split": split, "pair_log2": log2, "dense_slots": dense, "pair_max_ops": cap}
                 got = _with_options(opts, lambda: gp.batch_count([g] * len(scheds), scheds))
-                assert got == want, (split, log2, dense)
+                assert got == want, (split, log2, dense, cap)
         assert _with_options({"pair_leaf": 0}, lambda: gp.batch_count([g] * len(scheds), scheds)) == want
 
 
