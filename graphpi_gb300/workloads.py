@@ -66,3 +66,83 @@ def uneven_params(count: int = 256, first_seed: int = 100, n_lo: int = 1000, n_h
 def uneven_graph(n: int, avg: float, gamma: float, seed: int) -> api.Graph:
     # average degree can't exceed n - 1; cap weights at n / 2
     return api.chung_lu(n, min(avg, (n - 1) / 2.0), gamma, max(2, n // 2), seed)
+
+
+def uneven_benchmark(count: int = 256, steps: int = 3, step_seconds: float = 2.0) -> dict:
+    """The uneven batch: `count` Chung-Lu graphs, one motif each, counted in
+    one persistent launch per step against one launch per (pattern, graph)
+    pair over the same stripe of the work.  The stripe count is the smallest
+    power of two (from 2^16 down) whose batched launch stays near
+    `step_seconds`; both legs must give the same raw sums."""
+    import ctypes as C
+    import statistics
+    import time
+
+    from . import native
+    from .native import U128, check, lib
+
+    motifs = api.motifs_3_to_5()
+    t0 = time.time()
+    graphs, scheds = [], []
+    for n, avg, gamma, seed, m in uneven_params(count):
+        g = uneven_graph(n, avg, gamma, seed)
+        graphs.append(g)
+        scheds.append(api.Schedule(motifs[m], 1, 1, True, g.v_cnt, g.e_cnt, g.triangle_counting_mt()))
+    plans = [api.Plan(s) for s in scheds]
+    gh = (C.c_void_p * count)(*[g.device() for g in graphs])
+    ph = (C.c_void_p * count)(*[p.handle for p in plans])
+    red = [s.get_in_exclusion_optimize_redundancy() for s in scheds]
+    setup_s = time.time() - t0
+
+    def batched(S: int, stripe: int) -> tuple[float, list[int]]:
+        native.set_option("stripes", S)
+        native.set_option("stripe", stripe)
+        outs = (U128 * count)()
+        check(lib().gpm_batch_count(count, gh, ph, outs), "gpm_batch_count")
+        return native.last_launch_stats()[0], [o.value for o in outs]
+
+    native.set_option("raw_sums", 1)
+    try:
+        S = 1 << 16
+        while True:
+            t, _ = batched(S, S - 1)
+            if t >= step_seconds * 1e3 / 4 or S == 1:
+                break
+            S //= 2
+        while S > 1 and t * 2 <= step_seconds * 1e3:
+            S //= 2
+            t *= 2
+        for i in range(3):
+            batched(S, steps + i)
+        b_ms, p_ms, emb = [], [], 0.0
+        for i in range(steps):
+            ms, raw = batched(S, i)
+            b_ms.append(ms)
+            signed = [r - (1 << 128) if r >= (1 << 127) else r for r in raw]
+            emb += sum(r / d for r, d in zip(signed, red))
+            tot = 0.0
+            for j in range(count):
+                o = U128()
+                check(lib().gpm_count(gh[j], ph[j], C.byref(o)), "gpm_count")
+                tot += native.last_launch_stats()[0]
+                if o.value != raw[j]:
+                    raise AssertionError(f"pair {j}: one-pair launch and batch differ")
+            p_ms.append(tot)
+    finally:
+        native.set_option("stripes", 1)
+        native.set_option("stripe", 0)
+        native.set_option("raw_sums", 0)
+    return {"workload": f"uneven batch, {count} Chung-Lu graphs (1k-200k vertices), one motif each",
+            "stripes": S, "steps": steps, "batched_ms_per_step": statistics.median(b_ms),
+            "plain_ms_per_step": statistics.median(p_ms),
+            "batched_speedup_vs_plain": statistics.median(p_ms) / statistics.median(b_ms),
+            "embeddings_per_s": emb / (sum(b_ms) / 1e3), "vertices": sum(g.v_cnt for g in graphs),
+            "directed_edges": sum(g.e_cnt for g in graphs), "setup_s": setup_s}
+
+
+if __name__ == "__main__":
+    import json
+    import sys
+
+    if len(sys.argv) > 1 and sys.argv[1] == "uneven":
+        print(json.dumps(uneven_benchmark(int(sys.argv[2]) if len(sys.argv) > 2 else 256)))
