@@ -227,7 +227,13 @@ Schedule::Schedule(const Pattern& pattern, bool& is_pattern_valid, int performan
             if (performance_modeling_type == 2) return GraphZero_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
             return Naive_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
         };
-        for (const auto& order : candidates) {
+        // Every order is scored independently (in parallel); the choice is
+        // the reference's sequential one: the first strict minimum in order.
+        std::vector<double> order_val(candidates.size());
+        std::vector<PairList> order_pairs(candidates.size());
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long i = 0; i < (long)candidates.size(); ++i) {
+            const std::vector<int>& order = candidates[i];
             std::vector<int> cur = reorder(pattern.get_adj_mat_ptr(), n, order);
             std::vector<PairList> options;
             if (restricts_type == 1) {
@@ -238,23 +244,26 @@ Schedule::Schedule(const Pattern& pattern, bool& is_pattern_valid, int performan
                 probe.GraphZero_aggressive_optimize(pairs);
                 options.push_back(pairs);
             }
+            bool have = false;
             if (options.empty()) {
-                double val = score(order, PairList());
-                if (!have_best || val < min_val) {
-                    have_best = true;
-                    min_val = val;
-                    best_order = order;
-                    best_pairs.clear();
-                }
+                order_val[i] = score(order, PairList());
+                have = true;
             }
             for (const auto& pairs : options) {
-                double val = score(order, pairs);
-                if (!have_best || val < min_val) {
-                    have_best = true;
-                    min_val = val;
-                    best_order = order;
-                    best_pairs = pairs;
+                const double val = score(order, pairs);
+                if (!have || val < order_val[i]) {
+                    have = true;
+                    order_val[i] = val;
+                    order_pairs[i] = pairs;
                 }
+            }
+        }
+        for (size_t i = 0; i < candidates.size(); ++i) {
+            if (!have_best || order_val[i] < min_val) {
+                have_best = true;
+                min_val = order_val[i];
+                best_order = candidates[i];
+                best_pairs = order_pairs[i];
             }
         }
         adj_mat = reorder(pattern.get_adj_mat_ptr(), n, best_order);
@@ -366,7 +375,11 @@ std::vector<Schedule::Candidate> Schedule::candidates(const Pattern& pattern, in
         if (perf == 3) return probe.Naive_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
         return probe.our_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt, tri_cnt);
     };
-    for (const auto& order : cands) {
+    // orders scored in parallel, listed in the reference's order
+    std::vector<std::vector<Candidate> > per(cands.size());
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long i = 0; i < (long)cands.size(); ++i) {
+        const std::vector<int>& order = cands[i];
         std::vector<int> cur = reorder(pattern.get_adj_mat_ptr(), n, order);
         std::vector<PairList> options;
         if (restricts_type == 1) {
@@ -378,8 +391,9 @@ std::vector<Schedule::Candidate> Schedule::candidates(const Pattern& pattern, in
             options.push_back(pairs);
         }
         if (options.empty()) options.push_back(PairList());
-        for (const auto& pairs : options) out.push_back(Candidate{order, pairs, score(order, pairs)});
+        for (const auto& pairs : options) per[i].push_back(Candidate{order, pairs, score(order, pairs)});
     }
+    for (auto& v : per) out.insert(out.end(), v.begin(), v.end());
     return out;
 }
 
@@ -547,15 +561,37 @@ void Schedule::aggressive_optimize_get_all_pairs(std::vector<std::vector<std::pa
     restriction_dfs(base_dag, iso, groups, pairs, ordered_pairs_vector);
 }
 
+// Orderings of n distinct values that satisfy every pair (value[second] <
+// value[first]): a subset DP that assigns the values from the smallest up.
+static long long linear_extensions(int n, const std::vector<std::pair<int, int> >& pairs) {
+    unsigned below[8] = {0};
+    for (const auto& p : pairs) below[p.first] |= 1u << p.second;
+    std::vector<long long> ways((size_t)1 << n, 0);
+    ways[0] = 1;
+    for (unsigned mask = 0; mask < (1u << n); ++mask) {
+        if (!ways[mask]) continue;
+        for (int v = 0; v < n; ++v)
+            if (!(mask >> v & 1) && (below[v] & ~mask) == 0) ways[mask | (1u << v)] += ways[mask];
+    }
+    return ways[((size_t)1 << n) - 1];
+}
+
+// Keeps the restriction sets under which the pattern is counted exactly once
+// per embedding.  The reference decides it by counting on the complete graph
+// K_{n+1} with and without the set (src/schedule.cpp:1433-1456).  On a
+// complete graph every injective map is an embedding, so those counts are
+// (n+1)! / |Aut| (all maps, one per automorphism class) and (n+1) x the
+// number of orderings of n values the set allows: the test is exactly
+// linear_extensions(set) x |Aut| == n!, decided here without enumerating.
 void Schedule::restricts_generate(const int* cur_adj_mat, std::vector<std::vector<std::pair<int, int> > >& restricts) {
     Schedule base(cur_adj_mat, size);
     base.aggressive_optimize_get_all_pairs(restricts);
     const int n = base.get_size();
-    const long long expected = complete_graph_count(base, n + 1) / base.get_multiplicity();
+    long long fact = 1;
+    for (int i = 2; i <= n; ++i) fact *= i;
+    const long long aut = base.get_multiplicity();
     for (size_t i = 0; i < restricts.size();) {
-        Schedule trial(base.get_adj_mat_ptr(), n);
-        trial.add_restrict(restricts[i]);
-        if (complete_graph_count(trial, n + 1) != expected) restricts.erase(restricts.begin() + i);
+        if (linear_extensions(n, restricts[i]) * aut != fact) restricts.erase(restricts.begin() + i);
         else ++i;
     }
 }
