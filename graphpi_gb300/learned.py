@@ -200,10 +200,12 @@ class CostModel:
 
 
 def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = True,
-           judge: int = 0) -> tuple[Schedule, dict]:
+           judge: int = 0, shortlist: int = 0) -> tuple[Schedule, dict]:
     """Learned schedule choice (analytic model when model is None).  With
-    judge=k the k candidates the model ranks fastest and the analytic choice
-    are timed on a sample of the work and the fastest measured one wins."""
+    shortlist=s the model only re-ranks the s analytically cheapest
+    candidates.  With judge=k the k candidates the model ranks fastest and
+    the analytic choice are timed on a sample of the work and the fastest
+    measured one wins."""
     stats = graph_stats(g)
     cands = schedule_candidates(pattern, 1, 1, stats["v_cnt"], stats["e_cnt"], stats["tri_cnt"])
     if model is None:
@@ -213,6 +215,9 @@ def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = 
     scheds = [schedule_from_order(pattern, c["order"], c["pairs"], use_iep, 1) for c in cands]
     feats = relativize(np.stack([schedule_features(s, stats, c["cost"]) for s, c in zip(scheds, cands)]))
     pred = model.predict(feats)
+    if shortlist > 0:  # the model re-ranks the analytically cheapest candidates
+        keep = sorted(range(len(cands)), key=lambda j: (cands[j]["cost"], j))[:shortlist]
+        pred = np.array([pred[j] if j in keep else np.inf for j in range(len(cands))], dtype=np.float64)
     if judge <= 0:
         i = int(np.argmin(pred))
         return scheds[i], {"index": i, "by": "mlp", "pred_rel_log10_ms": float(pred[i])}
@@ -224,29 +229,33 @@ def choose(pattern: Pattern, g: Graph, model: CostModel | None, use_iep: bool = 
     return scheds[i], {"index": i, "by": "mlp+measured", "timed_ms": timed, "analytic_index": a}
 
 
-def evaluate(rows: list[dict], model: CostModel, judge: int = 3) -> dict:
-    """Per pattern: measured time of the MLP's pick, of the judged pick (the
-    fastest measured among the MLP's top `judge` and the analytic choice),
-    of the analytic pick, and of the best candidate (from measured rows)."""
+def evaluate(rows: list[dict], model: CostModel, judge: int = 3, shortlist: int = 4) -> dict:
+    """Per pattern: measured time of the MLP's pick over all candidates, of
+    its pick among the `shortlist` analytically cheapest ("rerank"), of the
+    judged pick (the fastest measured among the MLP's top `judge` and the
+    analytic choice), of the analytic pick, and of the best candidate."""
     by_pat: dict[int, list[dict]] = {}
     for r in rows:
         by_pat.setdefault(r["pattern"], []).append(r)
-    tot = {"mlp": 0.0, "judged": 0.0, "analytic": 0.0, "best": 0.0}
+    tot = {"mlp": 0.0, "rerank": 0.0, "judged": 0.0, "analytic": 0.0, "best": 0.0}
     per = []
     for pi, rs in sorted(by_pat.items()):
         pred = model.predict(np.stack([r["features"] for r in rs]))
         order = np.argsort(pred)
         m = rs[int(order[0])]["ms"]
-        ra = min(rs, key=lambda r: (r["cost"], r["cand"]))
-        a = ra["ms"]
+        by_cost = sorted(range(len(rs)), key=lambda i: (rs[i]["cost"], rs[i]["cand"]))
+        a = rs[by_cost[0]]["ms"]
+        short = by_cost[:shortlist]
+        rr = rs[min(short, key=lambda i: (pred[i], i))]["ms"]
         j = min([rs[int(i)]["ms"] for i in order[:judge]] + [a])
         b = min(r["ms"] for r in rs)
         tot["mlp"] += m
+        tot["rerank"] += rr
         tot["judged"] += j
         tot["analytic"] += a
         tot["best"] += b
-        per.append({"pattern": pi, "mlp_ms": m, "judged_ms": j, "analytic_ms": a, "best_ms": b})
-    for k in ("mlp", "judged", "analytic"):
+        per.append({"pattern": pi, "mlp_ms": m, "rerank_ms": rr, "judged_ms": j, "analytic_ms": a, "best_ms": b})
+    for k in ("mlp", "rerank", "judged", "analytic"):
         tot[f"{k}_over_best"] = tot[k] / max(tot["best"], 1e-9)
     tot["per_pattern"] = per
     return tot
@@ -285,9 +294,10 @@ def main(argv: list[str] | None = None) -> dict:
     ev = evaluate(rows_ev, model)
     res = {"train_graph": f"rmat s{a.train_scale}", "eval_graph": f"rmat s{a.eval_scale}",
            "train_rows": len(rows_tr), "eval_rows": len(rows_ev), "train_loss": loss,
-           "mlp_over_best": ev["mlp_over_best"], "judged_over_best": ev["judged_over_best"],
-           "analytic_over_best": ev["analytic_over_best"],
-           "mlp_ms": ev["mlp"], "judged_ms": ev["judged"], "analytic_ms": ev["analytic"], "best_ms": ev["best"],
+           "mlp_over_best": ev["mlp_over_best"], "rerank_over_best": ev["rerank_over_best"],
+           "judged_over_best": ev["judged_over_best"], "analytic_over_best": ev["analytic_over_best"],
+           "mlp_ms": ev["mlp"], "rerank_ms": ev["rerank"], "judged_ms": ev["judged"], "analytic_ms": ev["analytic"],
+           "best_ms": ev["best"],
            "per_pattern": ev["per_pattern"], "seconds": time.time() - t0}
     model.close()
     text = json.dumps(res, indent=1)

@@ -91,10 +91,13 @@ def test_learned_choice_exact_and_reported(engine, oracle):
     assert ev["mlp_over_best"] >= 1.0 and ev["analytic_over_best"] >= 1.0
     # measured runtime judges the model's shortlist, which holds the analytic choice
     assert ev["judged_over_best"] <= ev["analytic_over_best"] + 1e-9
+    assert ev["rerank_over_best"] >= 1.0
     # whatever is chosen counts exactly
     tri = g.triangle_counting_mt()
     for p in held[:4]:
         s_mlp, _ = learned.choose(p, g, model)
+        s_rr, _ = learned.choose(p, g, model, shortlist=4)
+        assert g.pattern_matching(s_rr) == oracle.count(g, s_rr)
         s_jdg, info = learned.choose(p, g, model, judge=2)
         assert info["analytic_index"] in info["timed_ms"]
         s_ref = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri)
