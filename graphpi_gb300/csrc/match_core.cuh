@@ -1172,12 +1172,11 @@ struct WarpCtx {
     }
 
     // After the warp's own queues: helps published loops until every warp
-    // is done, or no record has had slices left for kIdleRounds scans in a
-    // row (so helpers never hold SMs that blocks not yet resident need).
+    // is done.  The host clamps the grid to the blocks that are resident at
+    // once, so every other warp is running and the wait ends when they do;
+    // the polling is bounded all the same (2^22 rounds of at least 16 us).
     __device__ void help_all(const PairDesc* pairs, int npairs, unsigned long long* out, unsigned total_warps) {
-        constexpr unsigned kIdleRounds = 4096;
-        unsigned idle = 0;
-        for (unsigned round = 0; round < (1u << 24) && idle < kIdleRounds; ++round) {
+        for (unsigned round = 0; round < (1u << 22); ++round) {
             bool worked = false;
             for (int base = 0; base < kDonSlots; base += 32) {
                 const int h = (int)((gw * 37 + base + lane) & (kDonSlots - 1));
@@ -1192,16 +1191,12 @@ struct WarpCtx {
                     if (help_one(pairs, npairs, out, hj, (unsigned)(wj >> 48))) worked = true;
                 }
             }
-            if (worked) {
-                idle = 0;
-                continue;
-            }
+            if (worked) continue;
             // one lane reads the counter: the exit must be warp-uniform
             unsigned fin = 0;
             if (lane == 0) fin = *(volatile unsigned*)&don->finished;
             if (__shfl_sync(kFull, fin, 0) >= total_warps) return;
-            ++idle;
-            __nanosleep(4000);
+            __nanosleep(16000);
         }
     }
 
