@@ -1275,7 +1275,12 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match
     w.bm = bitmaps ? bitmaps + (size_t)gw * 2 * (size_t)bm_words : nullptr;
     w.bm_words = bm_words;
     w.bm_min = bm_min;
-    for (int p = 0; p < npairs; ++p) {
+    // Each warp starts at its own pair (warp index mod pairs) and then visits
+    // all of them, so the heavy pairs' tasks start at once instead of after
+    // every warp has worked through the pairs before them.
+    const int p0 = (int)(gw % npairs);
+    for (int k = 0; k < npairs; ++k) {
+        const int p = p0 + k < npairs ? p0 + k : p0 + k - npairs;
         const PairDesc pd = pairs[p];
         w.P = pd.plan;
         w.g = pd.g;
