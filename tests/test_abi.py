@@ -98,3 +98,16 @@ def test_workload_params_stable():
     assert all(1000 <= n <= 200000 and 4 <= avg <= 64 and 2.0 <= gm <= 2.8 and 0 <= m < 29
                for n, avg, gm, _, m in ps)
     assert ps == workloads.uneven_params()
+
+
+def test_engine_defaults_and_option_checks(engine):
+    # the shipped defaults (each chosen by measurement) and the range checks
+    want = {"split": 64, "pair_leaf": 1, "leaf_batch": 0, "dense_slots": 0, "pair_max_ops": 0, "bitmap_min": 4096,
+            "min_blocks": 1, "stripes": 1, "stripe": 0, "raw_sums": 0, "pair_log2": 0}
+    for k, v in want.items():
+        assert gp.get_option(k) == v, k
+    for bad in (("min_blocks", 2), ("split", -1), ("pair_log2", 25), ("stripes", 0), ("no_such_knob", 1)):
+        with pytest.raises(gp.GpmError):
+            gp.set_option(*bad)
+    for k, v in want.items():
+        assert gp.get_option(k) == v, k
