@@ -224,8 +224,10 @@ void expect_oracle(const char* what, const Csr& g, const std::vector<Sched>& ss,
                                     o))
             std::abort();
         const unsigned __int128 want = ((unsigned __int128)o[1] << 64) | o[0];
+        // the host divides the raw sum by the redundancy as the reference does
+        // (for label-sensitive plans the reference's raw sum is not a multiple)
         const unsigned __int128 got = (unsigned __int128)(raw[i] / (__int128)ss[i].plan.redundancy);
-        if (got != want || raw[i] % (__int128)ss[i].plan.redundancy != 0) {
+        if (got != want) {
             std::printf("MISMATCH %s pair %zu: got %llu want %llu (split %d leaf %d pair %d)\n", what, i,
                         (unsigned long long)got, (unsigned long long)want, k.split, k.leaf, k.pair);
             ++failures;
