@@ -276,15 +276,17 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
  *   "split" (a loop at depth >= 2 with at least this many candidates is
  *   published so that idle warps take slices of it; 0 = off),
  *   "stage_max" (largest father set staged in shared memory),
- *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan allows;
- *   the pair-sum leaf is on by default, the batched leaf off), "pair_log2" (entries per warp of the pair-sum
- *   table as a power of two; 0 = sized to free memory), "dense_slots"
- *   (per-vertex counter arrays shared by pair sums too big for the table;
- *   default 0 = none), "bitmap_min"
- *   (fixed leaf sets at least this large are tested through a per-warp
- *   bitmap instead of a binary search; 0 = never),
+ *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan
+ *   allows; the pair-sum leaf is on by default, the batched leaf off),
+ *   "pair_log2" (entries per warp of the pair-sum table as a power of two;
+ *   0 = sized to free memory), "pair_max_ops" (longest pair sum one warp
+ *   takes on, in list elements; longer ones run as loops; 0 = no cap),
+ *   "dense_slots" (per-vertex counter arrays shared by pair sums too big for
+ *   the table; default 0 = none), "bitmap_min" (fixed leaf sets at least
+ *   this large are tested through a per-warp bitmap instead of a binary
+ *   search; 0 = never),
  *   "merge_alpha4_small"/"_mid"/"_large" (merge vs search per length bucket),
- *   "timeout_ms" (bounded waits),
+ *   "timeout_ms" (reserved; no engine wait reads it),
  *   "stripes"/"stripe" (a launch covers only the first-level tasks t with
  *   t mod stripes == stripe: the tasks split into `stripes` interleaved
  *   parts, e.g. one per GPU or per bounded step), "raw_sums" (1: outputs are the undivided
