@@ -328,6 +328,23 @@ void case_stripes() {
             ++failures;
         }
     }
+    // the stripes of a job (one per rank, say) add up to the whole job
+    Knobs all;
+    all.split = 2;
+    const std::vector<__int128> whole = launch(g, ss, all);
+    std::vector<__int128> sum(ss.size(), 0);
+    for (unsigned long long st = 0; st < 4; ++st) {
+        Knobs k;
+        k.split = 2;
+        k.stripes = 4;
+        k.stripe = st;
+        const std::vector<__int128> r = launch(g, ss, k);
+        for (size_t i = 0; i < r.size(); ++i) sum[i] += r[i];
+    }
+    if (sum != whole) {
+        std::printf("MISMATCH stripes: the four stripes do not add up to the whole job\n");
+        ++failures;
+    }
     std::printf("ok stripes\n");
 }
 

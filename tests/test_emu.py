@@ -3,10 +3,11 @@ compiled as host C++ against the warp emulator (tests/emu/warp_emu.h) with
 AddressSanitizer, run on small skewed graphs and compared with the oracle.
 
 Covers, without a GPU: loop donation with every loop shared (split=1, the
-most racy setting) with and without the batched leaf, the pair-sum leaf, and
-stripes that do not depend on the grab size; any out-of-bounds access, any
-lane that meets a different shuffle/ballot/syncwarp than its warp, and any
-internal check stops the run."""
+most racy setting) with and without the batched leaf, the pair-sum leaf and
+its dense counter arrays, leaf bitmaps, stripes that do not depend on the
+grab size and that add up to the whole job (the multi-rank split); any
+out-of-bounds access, any lane that meets a different shuffle/ballot/syncwarp
+than its warp, and any internal check stops the run."""
 import os
 import shutil
 import subprocess
