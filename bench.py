@@ -2,27 +2,43 @@
 R-MAT scale-22 graph (4,194,304 vertices, edge factor 16,
 a/b/c/d = .57/.19/.19/.05, seed 3), one persistent launch per step.
 
-A step is one launch over one stripe of the first-level work: the
-schedule-driven enumeration of all 29 motifs for the first-level tasks
-(root, first neighbour) t with t mod S = s, S stripes in all (the same
-interleaved partition that splits the job across GPUs).  S is fixed
-(2^23: about 15 edge tasks per motif per step) so that runs compare: the
-timed steps take stripes 0..K-1, the warm-up steps the next W.  The whole
-job is far beyond a benchmark window, and embeddings/s is dominated by the
-hub edges each stripe holds (the first tasks belong to the largest hub).
-The graph (0.5 GB of CSR, larger than the 129 MB L2) stays resident in HBM.
+A step is one stripe of the job's first-level tasks (the directed edges
+(v0, v1) of the degree-relabelled CSR, or root vertices for plans whose
+inclusion-exclusion tail starts at depth 1): the tasks t with t mod S = s,
+S = 2^23 stripes in all (about 15 tasks per motif per step), counted for all
+29 motifs in one launch.  The stripe ids are drawn uniformly at random from
+a seeded stream (workloads.random_stripes): the timed steps take ids[0..K),
+the warm-up steps ids[K..K+W).  A uniformly random stripe is an unbiased
+sample of the whole job, so embeddings/s over the steps estimates the whole
+job's throughput.  The graph (0.5 GB of CSR, larger than the 129 MB L2)
+stays resident in HBM.
+
+Schedules: the engine's Schedule (perf=1, restricts=1, IEP on) for the
+graph's v/e/tri counts; the bench checks that its tables equal the
+reference's own, recorded with the undivided sums of the reference itself
+over the first 48 stripe ids in tests/golden/bench_stripes.json.  Every
+timed stripe's raw sums are compared with those recorded sums, bit for bit.
 
 Reported on one JSON line (rank 0):
   value      embeddings/s over the timed steps, inputs resident in HBM
+             (one CUDA-graph replay of the batched launch per step)
   e2e        the same through gpm_count_host with pinned host buffers: upload,
              device relabel, count, download, free inside every step
   plain      the same stripes counted one pattern per launch (29 launches)
   roofline   algorithmic bytes of the intersections per launch / kernel time
-             against the measured HBM copy bandwidth
+             against the measured HBM copy bandwidth; DRAM bytes per launch
+             from a committed ncu capture beside it
   cpu_baseline  the CPU oracle (a restatement of the reference's OpenMP
-             pattern_matching) on a bounded root sample, all host cores
+             pattern_matching, split into the same first-level tasks) on the
+             first timed stripes, all host cores, sums checked equal
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--config c3|c2]
+
+--config c2: rectangle and house on R-MAT scale 20 (seed 2), one pattern
+per launch, a step = one random stripe of 2^16.
+--impl reference: the reference's CPU path (the oracle port, no GPU, without
+the engine library in the process) on exactly the same stripes.
 """
 from __future__ import annotations
 
@@ -44,6 +60,14 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "embeddings/s, batched 5-motif R-MAT s22 vs per-pattern GPU; HBM % peak; p50"
 HBM_FALLBACK_GBS = 6800.0
+GOLDEN = ROOT / "tests" / "golden" / "bench_stripes.json"
+
+CONFIGS = {
+    "c3": dict(scale=22, seed=3, golden="rmat_s22", stripes=1 << 23, batched=True,
+               workload="rmat_s22 x 29 motifs (3-5 vertices), batched persistent launch"),
+    "c2": dict(scale=20, seed=2, golden="rmat_s20", stripes=1 << 16, batched=False,
+               workload="rmat_s20 x {rectangle, house}, one pattern per launch"),
+}
 
 
 def _peak_hbm() -> tuple[float, str]:
@@ -104,11 +128,64 @@ def _signed(v: int) -> int:
     return v - (1 << 128) if v >= (1 << 127) else v
 
 
-def build_workload(gp, workloads, scale: int = 22):
-    t = time.time()
-    g = workloads.rmat_s22() if scale == 22 else workloads.rmat_scale(scale, 3)
-    gen_s = time.time() - t
-    return g, gen_s
+def load_golden(cfg: dict, g0=None) -> dict | None:
+    """The reference's recorded tables and stripe sums for this graph (None
+    when absent or recorded for another graph)."""
+    if not GOLDEN.exists():
+        return None
+    e = json.loads(GOLDEN.read_text()).get(cfg["golden"])
+    if e is None:
+        return None
+    if g0 is not None:
+        from tests.oracle_lib import csr_checksum
+        if csr_checksum(g0) != e["checksum"]:
+            raise AssertionError("the generated graph differs from the one the reference sums were recorded on")
+    return e
+
+
+def step_ids(args, S: int) -> tuple[list[int], list[int]]:
+    from graphpi_gb300 import workloads
+    ids = workloads.random_stripes(S, args.steps + args.warmup)
+    return ids[:args.steps], ids[args.steps:]
+
+
+def bench_config(args, cfg: dict, S: int) -> dict:
+    """The workload description both arms print (identical by construction)."""
+    return {
+        "workload": cfg["workload"],
+        "graph": f"R-MAT scale {cfg['scale']}, edge factor 16, (.57,.19,.19,.05), seed {cfg['seed']}, "
+                 "symmetrised, deduplicated, relabelled by degree",
+        "schedule": "perf=1, restricts=1, IEP on (tables equal to the reference's Schedule)",
+        "stripes": S,
+        "step": f"one seeded random stripe = 1/{S} of the first-level tasks "
+                f"(workloads.random_stripes: timed ids[0..{args.steps}), warm-up ids[{args.steps}..{args.steps + args.warmup}))",
+        "l2": "inputs larger than L2 (CSR of the graph vs 129 MB)",
+    }
+
+
+def check_against_golden(golden, ids: list[int], raws_by_step: list[list[int]]) -> int:
+    """Compares raw stripe sums with the reference's recorded ones (mod 2^64,
+    the reference's long long); returns how many stripes were checked."""
+    if golden is None:
+        return 0
+    pos = {s: j for j, s in enumerate(golden["ids"])}
+    checked = 0
+    for s, raws in zip(ids, raws_by_step):
+        j = pos.get(s)
+        if j is None:
+            continue
+        for i, r in enumerate(raws):
+            want = golden["raw"][i][j]
+            if (r - want) % (1 << 64) != 0:
+                raise AssertionError(f"stripe {s}, pattern {golden['names'][i]}: raw sum {r} != reference {want}")
+        checked += 1
+    return checked
+
+
+def patterns_for(gp, cfg: dict):
+    if cfg["batched"]:
+        return gp.motifs_3_to_5()
+    return [gp.Pattern(gp.PatternType.Rectangle), gp.Pattern(gp.PatternType.House)]
 
 
 def run_ours(args, rank: int, world: int) -> dict | None:
@@ -116,6 +193,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     import graphpi_gb300 as gp
     from graphpi_gb300 import native, workloads
 
+    cfg = CONFIGS[args.config]
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     native.check(gp.lib().gpm_set_device(dev), "gpm_set_device")
@@ -124,64 +202,66 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    g, gen_s = build_workload(gp, workloads, args.scale)
+    t = time.time()
+    g = workloads.rmat_scale(cfg["scale"], cfg["seed"])
+    gen_s = time.time() - t
+    golden = load_golden(cfg, g)
     t = time.time()
     g.device()
     upload_s = time.time() - t
     tri = g.triangle_counting_mt()
-    pats = gp.motifs_3_to_5()
+    pats = patterns_for(gp, cfg)
     scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in pats]
+    tables_equal = None
+    if golden is not None:
+        if tri != golden["tri_cnt"]:
+            raise AssertionError(f"GPU triangle count {tri} != reference {golden['tri_cnt']}")
+        tables_equal = all([int(x) for x in s.tables] == want for s, want in zip(scheds, golden["tables"]))
+        if not tables_equal:
+            raise AssertionError("engine schedule tables differ from the reference's")
     red = [s.get_in_exclusion_optimize_redundancy() for s in scheds]
-    from graphpi_gb300 import autotune
-    tuned = autotune.apply_stored(g, scheds) if not args.no_tuning else None
-    plans = [gp.Plan(s) for s in scheds]
-    n = len(plans)
-    gh = (C.c_void_p * n)(*([g.device()] * n))
-    ph = (C.c_void_p * n)(*[p.handle for p in plans])
+    n = len(scheds)
+    S = args.stripes or cfg["stripes"]
+    timed_ids, warm_ids = step_ids(args, S)
+    # rank r takes every world-th step of the sequence
+    timed_ids = timed_ids[rank::world]
     gp.set_option("raw_sums", 1)
+    gp.set_option("stripes", S)
     gp.set_option("pair_log2", args.pair_log2)
     if args.leaf_batch is not None:
         gp.set_option("leaf_batch", args.leaf_batch)
     if args.pair_max_ops is not None:
         gp.set_option("pair_max_ops", args.pair_max_ops)
+    plans = [gp.Plan(s) for s in scheds]
+    gh = (C.c_void_p * n)(*([g.device()] * n))
+    ph = (C.c_void_p * n)(*[p.handle for p in plans])
+
+    exec_h = C.c_void_p()
 
     def batched(stripe: int) -> list[int]:
         gp.set_option("stripe", stripe)
         outs = (native.U128 * n)()
-        native.check(gp.lib().gpm_batch_count(n, gh, ph, outs), "gpm_batch_count")
+        native.check(gp.lib().gpm_batch_exec_run(C.byref(exec_h), n, gh, ph, outs), "gpm_batch_exec_run")
         return [_signed(o.value) for o in outs]
+
+    def per_pattern(stripe: int) -> tuple[list[int], list[float]]:
+        gp.set_option("stripe", stripe)
+        raws, ms = [], []
+        for p in plans:
+            o = native.U128()
+            native.check(gp.lib().gpm_count(g.device(), p.handle, C.byref(o)), "gpm_count")
+            raws.append(_signed(o.value))
+            ms.append(gp.last_launch_stats()[0])
+        return raws, ms
 
     def embeddings(raws) -> float:
         return sum(r / d for r, d in zip(raws, red))
 
-    # stripes for this rank: step i takes stripe (i * world + rank) mod S
-    def stripe_of(i: int) -> int:
-        return (i * world + rank) % S
-
-    if args.stripes == "auto":
-        # calibrate from the thinnest stripe (about one task per motif):
-        # double the work until a launch takes a quarter of --step-seconds,
-        # then extrapolate to a step of about --step-seconds (power of two)
-        want = args.step_seconds * 1e3
-        S = 1 << 27
-        while True:
-            gp.set_option("stripes", S)
-            batched(S - 1)
-            t = max(gp.last_launch_stats()[0], 1e-3)
-            print(f"[bench] calibrate: stripes={S} {t:.1f} ms", file=sys.stderr, flush=True)
-            if t >= want / 4 or S == 1:
-                break
-            S //= 2
-        while S > 1 and t * 2 <= want:
-            S //= 2
-            t *= 2
-    else:
-        S = int(args.stripes)
-    gp.set_option("stripes", S)
-    print(f"[bench] stripes={S}", file=sys.stderr, flush=True)
-    for i in range(args.warmup):
-        batched(stripe_of(args.steps + i))
-        print(f"[bench] warmup {i}: {gp.last_launch_stats()[0]:.1f} ms", file=sys.stderr, flush=True)
+    step = batched if cfg["batched"] else (lambda s: per_pattern(s)[0])
+    print(f"[bench] {cfg['workload']}: stripes={S}, timed ids {timed_ids[:4]}...", file=sys.stderr, flush=True)
+    for s in warm_ids:
+        step(s)
+        print(f"[bench] warmup stripe {s}: {gp.last_launch_stats()[0]:.1f} ms", file=sys.stderr, flush=True)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -189,9 +269,13 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clocks:
         e0.record()
-        for i in range(args.steps):
-            r = batched(stripe_of(i))
-            kernel_ms.append(gp.last_launch_stats()[0])
+        for s in timed_ids:
+            if cfg["batched"]:
+                r = batched(s)
+                kernel_ms.append(gp.last_launch_stats()[0])
+            else:
+                r, ms = per_pattern(s)
+                kernel_ms.append(sum(ms))
             raws_all.append(r)
             emb += embeddings(r)
         e1.record()
@@ -206,40 +290,61 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         dist.all_reduce(tt, op=dist.ReduceOp.SUM)
         elapsed_ms, emb = float(mx[0]), float(tt[1])
     value = emb / (elapsed_ms / 1e3)
+    print(f"[bench] timed: {elapsed_ms:.1f} ms for {len(timed_ids)} steps; kernel ms {kernel_ms}",
+          file=sys.stderr, flush=True)
+    checked = check_against_golden(golden, timed_ids, raws_all)
+    # exact 128-bit reduction of the ranks' raw sums (one host-side sum, no
+    # data-path collective); with every stripe recorded, it must equal the
+    # reference's total over all K stripes
+    from graphpi_gb300 import shard
+    totals = shard.reduce_raw_sums([sum(r[i] for r in raws_all) for i in range(n)], dist)
+    all_ids = step_ids(args, S)[0]
+    exact_total_checked = False
+    if golden is not None and golden["stripes"] == S and all(s in golden["ids"] for s in all_ids):
+        pos = {s: j for j, s in enumerate(golden["ids"])}
+        want = [sum(golden["raw"][i][pos[s]] for s in all_ids) for i in range(n)]
+        if totals != want:
+            raise AssertionError("rank-reduced raw totals differ from the reference's")
+        exact_total_checked = True
 
-    print(f"[bench] timed: {elapsed_ms:.1f} ms for {args.steps} steps", file=sys.stderr, flush=True)
     # ---- plain: one launch per pattern over the same stripes -------------
-    plain_ms, by_motif = [], [[] for _ in plans]
-    for i in range(args.steps):
-        gp.set_option("stripe", stripe_of(i))
-        tot = 0.0
-        for j, p in enumerate(plans):
+    plain_ms, by_pattern = [], [[] for _ in plans]
+    if cfg["batched"]:
+        for s, want in zip(timed_ids, raws_all):
+            raws, ms = per_pattern(s)
+            if raws != want:
+                raise AssertionError(f"stripe {s}: plain and batched counts differ")
+            plain_ms.append(sum(ms))
+            for j, m in enumerate(ms):
+                by_pattern[j].append(m)
+        print(f"[bench] plain: {[round(x, 1) for x in plain_ms]}", file=sys.stderr, flush=True)
+
+    # ---- algorithmic bytes of one launch (separate counting run) ----------
+    gp.set_option("count_bytes", 1)
+    algo_bytes = 0
+    if cfg["batched"]:
+        gp.set_option("stripe", timed_ids[0])
+        outs = (native.U128 * n)()
+        native.check(gp.lib().gpm_batch_count(n, gh, ph, outs), "gpm_batch_count")
+        algo_bytes = gp.last_launch_stats()[2]
+    else:
+        gp.set_option("stripe", timed_ids[0])
+        for p in plans:
             o = native.U128()
             native.check(gp.lib().gpm_count(g.device(), p.handle, C.byref(o)), "gpm_count")
-            ms = gp.last_launch_stats()[0]
-            tot += ms
-            by_motif[j].append(ms)
-            if _signed(o.value) != raws_all[i][j]:
-                raise AssertionError(f"plain and batched counts differ for motif {j}")
-        plain_ms.append(tot)
-
-    print(f"[bench] plain: {plain_ms}", file=sys.stderr, flush=True)
-    # ---- algorithmic bytes of one batched launch (separate counting run) ---
-    gp.set_option("count_bytes", 1)
-    batched(stripe_of(0))
-    _, _, algo_bytes = gp.last_launch_stats()
+            algo_bytes += gp.last_launch_stats()[2]
     gp.set_option("count_bytes", 0)
     k0 = kernel_ms[0]
     achieved = algo_bytes / (k0 / 1e3) / 1e9
     peak, peak_kind = _peak_hbm()
-    # DRAM bytes of one batched launch from the committed one-pass ncu capture
-    traffic, traffic_src = None, None
-    cap = ROOT / "profiles" / "match_kernel_dram.json"
-    if args.scale == 22 and cap.exists():
+    traffic, traffic_src, dram_frac = None, None, None
+    cap = ROOT / "profiles" / f"dram_{args.config}.json"
+    if cap.exists():
         c = json.loads(cap.read_text())
-        traffic = c.get("dram_bytes_per_launch")
-        traffic_src = f"ncu capture of stripe {c.get('stripe')} of {c.get('stripes')}, {c.get('knobs')}"
-
+        if c.get("stripes") == S and c.get("stripe") == timed_ids[0]:
+            traffic = c.get("dram_bytes_per_launch")
+            traffic_src = c.get("source")
+            dram_frac = traffic / (k0 / 1e3) / 1e9 / peak if traffic else None
 
     # ---- e2e through the host-buffer C ABI ---------------------------------
     vtx = torch.from_numpy(g.vertex.view(np.int32)).pin_memory()
@@ -249,8 +354,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     nw = np.array([len(t) for t in tabs], dtype=np.int32)
     e2e_emb, e2e_ms = 0.0, 0.0
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for i in range(args.steps):
-        gp.set_option("stripe", stripe_of(i))
+    for s, want in zip(timed_ids, raws_all):
+        gp.set_option("stripe", s)
         outs = (native.U128 * n)()
         torch.cuda.synchronize()
         h0.record()
@@ -259,112 +364,149 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         h1.record()
         torch.cuda.synchronize()
         e2e_ms += h0.elapsed_time(h1)
-        e2e_emb += embeddings([_signed(o.value) for o in outs])
+        got = [_signed(o.value) for o in outs]
+        if got != want:
+            raise AssertionError(f"stripe {s}: host-buffer path and resident path differ")
+        e2e_emb += embeddings(got)
+    gp.lib().gpm_batch_exec_destroy(exec_h)
     gp.set_option("stripes", 1)
     gp.set_option("stripe", 0)
     gp.set_option("raw_sums", 0)
 
     if rank != 0:
         return None
-    cpu = cpu_baseline(g, scheds, red, budget_s=args.cpu_budget) if args.cpu_budget > 0 else None
-    return {
+    cpu = cpu_baseline(g, scheds, red, S, timed_ids, raws_all, budget_s=args.cpu_budget) if args.cpu_budget > 0 else None
+    launches = len(timed_ids) * (1 if cfg["batched"] else n)
+    res = {
         "metric": METRIC,
         "value": value,
         "unit": "embeddings/s",
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": elapsed_ms / args.steps,
+        "ms_per_step": elapsed_ms / len(timed_ids),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "int32 CSR / int128 counts",
         "data": "synthetic (seeded R-MAT generator)",
-        "config": {
-            "workload": f"rmat_s{args.scale} x 29 motifs (3-5 vertices), batched persistent launch",
-            "graph": {"v_cnt": g.v_cnt, "e_cnt_directed": g.e_cnt,
-                      "generator": f"R-MAT scale {args.scale}, ef 16, (.57,.19,.19,.05), seed 3"},
-            "schedule": "perf=1, restricts=1, IEP on",
-            "stripes": S,
-            "tuning": ({k: v for k, v in tuned.items() if not k.startswith("_ms")} if tuned else "defaults"),
-            "step": f"one stripe = 1/{S} of the first-level tasks, all 29 motifs",
-            "l2": "inputs larger than L2 (0.5 GB CSR vs 129 MB)",
-            "gen_s": round(gen_s, 2),
-            "upload_relabel_s": round(upload_s, 3),
-        },
+        "config": bench_config(args, cfg, S),
+        "path": ("CUDA-graph replay of the batched launch (gpm_batch_exec_run)" if cfg["batched"]
+                 else "one gpm_count launch per pattern"),
         "kernel_ms_per_step": statistics.median(kernel_ms),
-        "plain_per_pattern_ms_per_step": statistics.median(plain_ms),
-        "plain_ms_by_motif": [round(sum(m), 2) for m in by_motif],
-        "batched_speedup_vs_plain": statistics.median(plain_ms) / statistics.median(kernel_ms),
-        "embeddings_per_step": emb / args.steps,
+        "kernel_ms_by_step": [round(x, 2) for x in kernel_ms],
+        "embeddings_per_step": emb / len(timed_ids),
+        "parity": {"schedule_tables_equal_reference": tables_equal, "tri_cnt_equal_reference": golden is not None,
+                   "stripes_checked_against_reference_sums": checked, "of": len(timed_ids),
+                   "rank_reduced_totals_equal_reference": exact_total_checked},
         "e2e": {"value": e2e_emb / (e2e_ms / 1e3), "unit": "embeddings/s",
                 "h2d_bytes_per_step": int(g.vertex.nbytes + g.edge.nbytes + flat.nbytes),
-                "d2h_bytes_per_step": 16 * n, "ms_per_step": e2e_ms / args.steps},
-        "gpu_launches": args.steps,
+                "d2h_bytes_per_step": 16 * n, "ms_per_step": e2e_ms / len(timed_ids)},
+        "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
-                     "peak_kind": peak_kind, "algo_bytes_per_launch": algo_bytes},
+                     "dram_frac": dram_frac, "peak_kind": peak_kind, "algo_bytes_per_launch": algo_bytes,
+                     "launch_stripe": timed_ids[0]},
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
+        "setup_s": {"generate": round(gen_s, 2), "upload_relabel": round(upload_s, 3)},
     }
+    if cfg["batched"]:
+        res["plain_per_pattern_ms_per_step"] = statistics.median(plain_ms)
+        res["plain_ms_by_motif"] = [round(sum(m), 2) for m in by_pattern]
+        res["batched_speedup_vs_plain"] = statistics.median(plain_ms) / statistics.median(kernel_ms)
+        res["batched_speedup_vs_plain_total"] = sum(plain_ms) / sum(kernel_ms)
+    return res
 
 
-def cpu_baseline(g, scheds, red, budget_s: float = 20.0, offset: int = 1, stride: int = 4096) -> dict:
-    """Oracle (port of the reference's OpenMP pattern_matching) on a bounded
-    root sample: roots offset, offset+stride, ... for every motif."""
+def _oracle_graph(g):
+    """The degree-relabelled host CSR: the numbering the engine's tasks use."""
+    from graphpi_gb300 import api
+    return api.relabel_by_degree(g)
+
+
+def cpu_baseline(g, scheds, red, S: int, ids: list[int], raws_all: list[list[int]], budget_s: float = 20.0) -> dict:
+    """The oracle (port of the reference's OpenMP pattern_matching, split into
+    the engine's first-level tasks) on the first timed stripes, one stripe at
+    a time until about budget_s of host time; sums must equal the GPU's."""
     from tests import oracle_lib
     orc = oracle_lib.load()
-    roots = np.arange(offset, g.v_cnt, stride, dtype=np.int32)
+    gr = _oracle_graph(g)
     threads = os.cpu_count() or 1
-    per_motif = budget_s / max(1, len(scheds))
+    tabs = [np.ascontiguousarray(s.tables, dtype=np.int64) for s in scheds]
     t0 = time.time()
-    emb, done_roots = 0.0, 0
-    for s, d in zip(scheds, red):
-        raw, done = orc.raw_roots_timed(g, s, roots, per_motif, threads)
-        emb += raw / d
-        done_roots += done
+    emb, used = 0.0, []
+    for s, want in zip(ids, raws_all):
+        got = [row[0] for row in orc.stripes_raw(gr, tabs, S, [s], threads)]
+        if got != want:
+            raise AssertionError(f"stripe {s}: CPU oracle and GPU raw sums differ")
+        emb += sum(r / d for r, d in zip(got, red))
+        used.append(s)
+        if time.time() - t0 >= budget_s:
+            break
     dt = time.time() - t0
     return {"value": emb / dt, "unit": "embeddings/s", "cores": threads, "kind": "port",
-            "sample": f"roots {offset} mod {stride} ({len(roots)} roots, {done_roots} root-motif runs finished "
-                      f"within {per_motif:.2f} s per motif), {len(scheds)} motifs, {dt:.1f} s",
+            "sample": f"stripes {used} of {S} (the first timed steps), {len(scheds)} patterns, {dt:.1f} s; "
+                      "raw sums equal to the GPU's",
             "seconds": dt}
 
 
 def run_reference(args, rank: int, world: int) -> dict | None:
-    """The reference's CPU path on the host cores.  The reference library is
-    compiled from its sources only where they exist; elsewhere its
-    restatement in oracle/oracle.c (same algorithm, 128-bit sums) runs."""
+    """The reference's CPU path on the host cores, on exactly the stripes the
+    GPU arm times.  The reference library is compiled from its sources only
+    where they exist, not on the GPU host, so its restatement in
+    oracle/oracle.c (same algorithm and task split, 128-bit sums) runs; the
+    graph comes from the generator library alone and the schedule tables are
+    the reference's own, recorded in tests/golden/bench_stripes.json, so the
+    engine library is never loaded in this process."""
     if rank != 0:
         return None
-    import graphpi_gb300 as gp
-    from graphpi_gb300 import workloads
-    g, _ = build_workload(gp, workloads, args.scale)
+    from graphpi_gb300 import api, workloads
     from tests import oracle_lib
+
+    cfg = CONFIGS[args.config]
+    g0 = workloads.rmat_scale(cfg["scale"], cfg["seed"])
+    golden = load_golden(cfg, g0)
+    if golden is None:
+        print(json.dumps({"impl": "reference", "unavailable": "tests/golden/bench_stripes.json has no "
+                          f"{cfg['golden']} entry (the reference's schedule tables for this graph)"}))
+        return None
+    g = api.relabel_by_degree(g0)
     orc = oracle_lib.load()
-    tri = orc.triangles(g, os.cpu_count() or 1)
-    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
-    red = [s.get_in_exclusion_optimize_redundancy() for s in scheds]
-    per_step = max(2.0, args.cpu_budget / 2)
-    for i in range(args.warmup):
-        cpu_baseline(g, scheds, red, budget_s=per_step / 4, offset=1 + 7 * (args.steps + i), stride=16384)
-    t0 = time.time()
-    emb = 0.0
-    samples = []
-    for i in range(args.steps):
-        r = cpu_baseline(g, scheds, red, budget_s=per_step, offset=1 + 7 * i, stride=4096)
-        emb += r["value"] * r["seconds"]
-        samples.append(r["sample"])
-    dt = time.time() - t0
-    value = emb / dt
+    tabs = [np.ascontiguousarray(t, dtype=np.int64) for t in golden["tables"]]
+    red = [int(t[-2]) for t in golden["tables"]]  # in_exclusion_optimize_redundancy
+    S = args.stripes or cfg["stripes"]
+    timed_ids, warm_ids = step_ids(args, S)
     threads = os.cpu_count() or 1
+    # warm-up: the same code on a 1/256 part of each warm-up stripe
+    for s in warm_ids:
+        orc.stripes_raw(g, tabs, S * 256, [s], threads)
+    t0 = time.time()
+    emb, per_step = 0.0, []
+    raws_all = []
+    for s in timed_ids:
+        ts = time.time()
+        got = [row[0] for row in orc.stripes_raw(g, tabs, S, [s], threads)]
+        per_step.append(time.time() - ts)
+        raws_all.append(got)
+        emb += sum(r / d for r, d in zip(got, red))
+        print(f"[reference] stripe {s}: {per_step[-1]:.2f} s", file=sys.stderr, flush=True)
+    dt = time.time() - t0
+    checked = check_against_golden(golden if S == golden["stripes"] else None, timed_ids, raws_all)
+    value = emb / dt
     return {
         "metric": METRIC, "value": value, "unit": "embeddings/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int64/int128 counts", "data": "synthetic (seeded R-MAT generator)",
-        "config": {"workload": f"rmat_s{args.scale} x 29 motifs (3-5 vertices)", "step": "bounded root sample per step"},
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / len(timed_ids), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32 CSR / int128 counts",
+        "data": "synthetic (seeded R-MAT generator)",
+        "config": bench_config(args, cfg, S),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "embeddings/s", "cores": threads, "kind": "port",
-                         "sample": samples[0]},
+                         "sample": f"the {len(timed_ids)} timed stripes of the GPU arm, every task counted "
+                                   f"({dt:.1f} s); schedule tables and sums from the reference itself "
+                                   f"(sums checked on {checked} stripes)"},
+        "parity": {"stripes_checked_against_reference_sums": checked, "of": len(timed_ids)},
+        "seconds_by_step": [round(x, 2) for x in per_step],
         "e2e": {"value": value, "unit": "embeddings/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -372,15 +514,12 @@ def run_reference(args, rank: int, world: int) -> dict | None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--stripes", default=os.environ.get("GPM_BENCH_STRIPES", str(1 << 23)),
-                    help="stripes per full job (a step is one stripe), or 'auto' to size a step to --step-seconds")
-    ap.add_argument("--step-seconds", type=float, default=4.0)
-    ap.add_argument("--scale", type=int, default=22, help="R-MAT scale (22 is the benchmark graph)")
+    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--stripes", type=int, default=0, help="stripes per full job (0: the config's)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--no-tuning", action="store_true", help="ignore the stored autotuner table")
     ap.add_argument("--pair-max-ops", type=int, default=None,
                     help="longest pair sum one warp takes on (default: the engine's)")
     ap.add_argument("--leaf-batch", type=int, default=None, choices=[0, 1],
@@ -394,8 +533,11 @@ def main() -> None:
         world = 1
     if args.warmup < 3:
         args.warmup = 3
-    import graphpi_gb300  # noqa: F401  (fails loudly when the engine is not built)
-    res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        import graphpi_gb300  # noqa: F401  (fails loudly when the engine is not built)
+        res = run_ours(args, rank, world)
     if rank == 0 and res is not None:
         print(json.dumps(res))
 

@@ -23,7 +23,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import native
-from .native import U128, check, lib
+from .native import U128, check, check_gen, gen_lib, lib
 
 
 class PatternType(enum.IntEnum):
@@ -225,6 +225,12 @@ class Schedule:
 
     # reference getters (include/schedule.h:23-37)
     def get_size(self): return self.size
+
+    def is_complete(self) -> bool:
+        """True for a clique pattern (every pair of vertices adjacent)."""
+        n = self.size
+        a = np.asarray(self.adj_mat).reshape(n, n)
+        return n >= 3 and bool(np.all(a + np.eye(n, dtype=a.dtype) >= 1))
     def get_total_prefix_num(self): return self.total_prefix_num
     def get_father_prefix_id(self, i): return self.father_prefix_id[i]
     def get_loop_set_prefix_id(self, i): return self.loop_set_prefix_id[i]
@@ -368,6 +374,14 @@ class Graph:
         return self.tri_cnt
 
     def pattern_matching(self, schedule: Schedule, thread_count: int = 0, clique: bool = False) -> int:
+        """Embeddings of the schedule's pattern (Graph::pattern_matching,
+        reference src/graph.cpp:199-245).  clique=True on a complete pattern
+        takes the clique fast path (gpm_clique_count); the count is the same
+        (the reference accepts the flag and counts the same way)."""
+        if clique and schedule.is_complete():
+            out = U128()
+            check(lib().gpm_clique_count(self.device(), schedule.get_size(), C.byref(out)), "gpm_clique_count")
+            return out.value
         plan = Plan(schedule)
         try:
             out = U128()
@@ -453,23 +467,23 @@ def _take_csr(rp, cl, n) -> tuple[np.ndarray, np.ndarray]:
     e = rp[n]
     vertex = np.ctypeslib.as_array(rp, shape=(n + 1,)).copy()
     edge = np.ctypeslib.as_array(cl, shape=(max(e, 1),))[:e].copy()
-    lib().gpm_free(C.cast(rp, C.c_void_p))
-    lib().gpm_free(C.cast(cl, C.c_void_p))
+    gen_lib().gpm_free(C.cast(rp, C.c_void_p))
+    gen_lib().gpm_free(C.cast(cl, C.c_void_p))
     return vertex, edge
 
 
 def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
          seed: int = 2) -> Graph:
     rp, cl, n = C.POINTER(C.c_uint32)(), C.POINTER(C.c_int32)(), C.c_int32()
-    check(lib().gpm_gen_rmat(scale, edge_factor, a, b, c, seed, C.byref(rp), C.byref(cl), C.byref(n)), "rmat")
+    check_gen(gen_lib().gpm_gen_rmat(scale, edge_factor, a, b, c, seed, C.byref(rp), C.byref(cl), C.byref(n)), "rmat")
     vertex, edge = _take_csr(rp, cl, n.value)
     return Graph(n.value, vertex, edge)
 
 
 def chung_lu(n: int, avg_degree: float, gamma: float, max_degree: int = 0, seed: int = 1) -> Graph:
     rp, cl, nv = C.POINTER(C.c_uint32)(), C.POINTER(C.c_int32)(), C.c_int32()
-    check(lib().gpm_gen_chung_lu(n, avg_degree, gamma, max_degree, seed, C.byref(rp), C.byref(cl), C.byref(nv)),
-          "chung_lu")
+    check_gen(gen_lib().gpm_gen_chung_lu(n, avg_degree, gamma, max_degree, seed, C.byref(rp), C.byref(cl),
+                                         C.byref(nv)), "chung_lu")
     vertex, edge = _take_csr(rp, cl, nv.value)
     return Graph(nv.value, vertex, edge)
 
@@ -493,16 +507,16 @@ def from_edges(v_cnt: int, src, dst, on_device: bool = False) -> Graph:
         g._dev = h
         return g
     rp, cl = C.POINTER(C.c_uint32)(), C.POINTER(C.c_int32)()
-    check(lib().gpm_csr_from_edges(v_cnt, len(s), s.ctypes.data, d.ctypes.data, C.byref(rp), C.byref(cl)),
-          "from_edges")
+    check_gen(gen_lib().gpm_csr_from_edges(v_cnt, len(s), s.ctypes.data, d.ctypes.data, C.byref(rp), C.byref(cl)),
+              "from_edges")
     vertex, edge = _take_csr(rp, cl, v_cnt)
     return Graph(v_cnt, vertex, edge)
 
 
 def relabel_by_degree(g: Graph) -> Graph:
     rp, cl = C.POINTER(C.c_uint32)(), C.POINTER(C.c_int32)()
-    check(lib().gpm_csr_relabel_degree(g.v_cnt, g.vertex.ctypes.data, g.edge.ctypes.data, C.byref(rp), C.byref(cl)),
-          "relabel")
+    check_gen(gen_lib().gpm_csr_relabel_degree(g.v_cnt, g.vertex.ctypes.data, g.edge.ctypes.data, C.byref(rp),
+                                               C.byref(cl)), "relabel")
     vertex, edge = _take_csr(rp, cl, g.v_cnt)
     return Graph(g.v_cnt, vertex, edge, g.tri_cnt)
 
@@ -537,11 +551,17 @@ class DataLoader:
 
     def load_data(self, data_type: DataType, path: str, oriented_type: int = 0) -> Graph | None:
         if data_type == DataType.Twitter:
-            raw = np.fromfile(path, dtype=np.uint32)
+            # header {v_cnt, e_cnt, max_degree}, vertex[v_cnt + 1], edge[e_cnt],
+            # little-endian uint32 (src/dataloader.cpp:165-190)
+            raw = np.fromfile(path, dtype="<u4")
+            if len(raw) < 4:
+                return None
             v, e = int(raw[0]), int(raw[1])
-            vertex = raw[3:4 + v].copy()
+            if len(raw) < 4 + v + e:
+                return None
+            vertex = raw[3:4 + v].astype(np.uint32)
             edge = raw[4 + v:4 + v + e].astype(np.int32)
-            if len(edge) != e or int(vertex[-1]) != e:
+            if int(vertex[0]) != 0 or int(vertex[-1]) != e:
                 return None
             return Graph(v, vertex, edge, _TRI[data_type])
         with open(path) as f:
@@ -567,7 +587,14 @@ class DataLoader:
             new_id = np.empty(v_hdr, dtype=np.int64)
             new_id[rank] = np.arange(v_hdr)
             ids = new_id[ids]
-        g = from_edges(v_hdr, ids[:, 0], ids[:, 1])
+        # the CSR is built on the GPU (gpm_graph_from_edges), on the host
+        # only when no CUDA device is present
+        try:
+            g = from_edges(v_hdr, ids[:, 0], ids[:, 1], on_device=True)
+        except native.GpmError as e:
+            if e.code != 7:  # GPM_ERR_NO_DEVICE
+                raise
+            g = from_edges(v_hdr, ids[:, 0], ids[:, 1])
         g.tri_cnt = _TRI.get(data_type, -1)
         return g
 

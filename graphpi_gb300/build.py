@@ -1,6 +1,10 @@
 """Builds the native library in-tree.
 
     graphpi_gb300/_lib/libgraphpi_gb300.so   engine: host C++ + sm_103a CUDA
+    graphpi_gb300/_lib/libgpm_gen.so         the seeded graph generators and host
+                                             CSR utilities alone (include/gpm_gen.h),
+                                             for processes that must not load the
+                                             engine (the CPU reference arm)
     oracle/liboracle.so                      CPU oracle (test infrastructure)
     oracle/_ref/libgraphpi_ref.so            reference GraphPi built from its own
                                              sources (only where they exist)
@@ -22,10 +26,14 @@ CSRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libgraphpi_gb300.so"
+GEN_LIB = LIBDIR / "libgpm_gen.so"
+GEN_SOURCES = ("gen", "errors")  # seeded generators + host CSR utilities (include/gpm_gen.h)
 ORACLE_SRC = ROOT / "oracle" / "oracle.c"
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 REF_SCRIPT = ROOT / "oracle" / "build_ref.sh"
-REFERENCE = Path("/root/reference")
+# the reference checkout the oracle/_ref recipe compiles from: GRAPHPI_REFERENCE,
+# else the checkout's usual location in the build container
+REFERENCE = Path(os.environ.get("GRAPHPI_REFERENCE", "/root/reference"))
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
@@ -81,6 +89,11 @@ def build_engine(force: bool = False) -> Path:
         _run_all([[nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fopenmp",
                    "-Xlinker", "-Bsymbolic", "-lgomp"]])
         os.replace(tmp, LIB)
+    gen_objs = [OBJ / (name + ".o") for name in GEN_SOURCES]
+    if force or _stale(GEN_LIB, gen_objs):
+        tmp = GEN_LIB.with_suffix(".so.tmp")
+        _run_all([["g++", "-shared", "-fopenmp", "-o", str(tmp), *map(str, gen_objs)]])
+        os.replace(tmp, GEN_LIB)
     return LIB
 
 

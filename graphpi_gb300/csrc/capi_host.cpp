@@ -1,4 +1,4 @@
-// Host half of the C ABI: errors, options, motif generation, the schedule
+// Host half of the C ABI: options, motif generation, the schedule
 // compiler entry point, and decoding schedule tables into a device plan.
 #include <algorithm>
 #include <cstdio>
@@ -13,19 +13,6 @@
 #include "graphpi/schedule.h"
 
 namespace gpm {
-
-static thread_local std::string g_last_error;
-
-void set_error(const char* fmt, ...) {
-    char buf[1024];
-    va_list ap;
-    va_start(ap, fmt);
-    vsnprintf(buf, sizeof buf, fmt, ap);
-    va_end(ap);
-    g_last_error = buf;
-}
-
-void clear_error() { g_last_error.clear(); }
 
 Options& options() {
     static Options o;
@@ -474,7 +461,6 @@ using gpm::set_error;
 
 extern "C" {
 
-GPM_API const char* gpm_last_error(void) { return gpm::g_last_error.c_str(); }
 
 GPM_API int gpm_motifs(int32_t k, int32_t* adj_out, int32_t cap, int32_t* count) {
     gpm::clear_error();

@@ -84,6 +84,99 @@ __global__ void __launch_bounds__(256) tc_kernel(GraphView g, unsigned long long
     if (lane == 0 && acc) atomicAdd(out, acc);
 }
 
+// k-clique counting, the clique fast path: Graph::pattern_matching_func with
+// clique = true (src/graph.cpp:147-197) and VertexSet::intersection's
+// min_vertex clip (src/vertex_set.cpp:75-103) for a complete pattern.  Every
+// clique is counted once, as its decreasing vertex sequence v0 > v1 > ...:
+// a task is a directed edge (v0, v1) with v1 < v0, S0 = N(v0) ∩ N(v1) below
+// v1, and below that S_{d+1} = S_d[0, i) ∩ N(S_d[i]) — the members of S_d
+// before position i are exactly those below S_d[i], so the clip is an index.
+// The last level counts |S_d[0, i) ∩ N(S_d[i])| without writing it.  No
+// restriction bounds or injectivity checks are needed: the order implies
+// both.  One warp per task; sets of level d live in the warp's scratch slot d.
+__global__ void __launch_bounds__(256) clique_kernel(GraphView g, int k, unsigned long long* __restrict__ cursor,
+                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch,
+                                                     int cap, int chunk, const unsigned long long* __restrict__ params) {
+    const unsigned long long stripes = params[0], stripe = params[1];
+    const int lane = threadIdx.x & 31;
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int* base = scratch + (size_t)gw * (size_t)max(1, k - 3) * (size_t)cap;
+    __int128 acc = 0;
+    int cur_v = -1;
+    unsigned cur_lo = 0, cur_hi = 0;
+    int idx[kMaxN], len[kMaxN];
+    for (;;) {
+        unsigned long long q = 0;
+        if (lane == 0) q = atomicAdd(cursor, 1ull);
+        q = __shfl_sync(kFull, q, 0);
+        const unsigned long long i0 = q * (unsigned long long)chunk;
+        if (i0 * stripes + stripe >= g.e_cnt) break;
+        for (unsigned long long i = i0; i < i0 + (unsigned long long)chunk; ++i) {
+            const unsigned long long t = i * stripes + stripe;
+            if (t >= g.e_cnt) break;
+            const unsigned e = (unsigned)t;
+            if (cur_v < 0 || e < cur_lo || e >= cur_hi) {
+                int lo = 0, hi = g.v_cnt;
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (g.rowptr[mid] <= e) lo = mid;
+                    else hi = mid - 1;
+                }
+                cur_v = lo;
+                cur_lo = g.rowptr[lo];
+                cur_hi = g.rowptr[lo + 1];
+            }
+            const int v1 = g.col[e];
+            if ((unsigned)v1 >= (unsigned)g.v_cnt) {
+                if (lane == 0) record_check(kErrBadVertex, e, v1, cur_v, g.v_cnt, 0, 0);
+                continue;
+            }
+            if (v1 >= cur_v) continue;
+            const int* n0 = g.col + cur_lo;
+            const int* n1 = g.col + g.rowptr[v1];
+            const int d1 = (int)(g.rowptr[v1 + 1] - g.rowptr[v1]);
+            if (k == 3) {
+                acc += isect_count(n0, (int)(cur_hi - cur_lo), n1, d1, v1, nullptr, 0, lane);
+                continue;
+            }
+            const int na = lower_bound_u(n0, (int)(cur_hi - cur_lo), v1);
+            const int nb = lower_bound_u(n1, d1, v1);
+            if (min(na, nb) > cap) {
+                if (lane == 0) record_check(kErrSetSize, -1, na, nb, cap, 0, 0);
+                continue;
+            }
+            len[0] = isect_store(n0, na, n1, nb, base, lane);
+            idx[0] = 0;
+            int d = 0;
+            while (d >= 0) {
+                if (idx[d] >= len[d]) {
+                    --d;
+                    continue;
+                }
+                const int* S = base + (size_t)d * cap;
+                const int pos = idx[d]++;
+                const int w = S[pos];
+                if ((unsigned)w >= (unsigned)g.v_cnt) {
+                    if (lane == 0) record_check(kErrBadVertex, w, g.v_cnt, k, d, 0, 0);
+                    continue;
+                }
+                const int* nw = g.col + g.rowptr[w];
+                const int dw = (int)(g.rowptr[w + 1] - g.rowptr[w]);
+                if (d == k - 4) {  // the last vertex: count, do not store
+                    acc += isect_count(S, pos, nw, dw, w, nullptr, 0, lane);
+                    continue;
+                }
+                len[d + 1] = isect_store(S, pos, nw, lower_bound_u(nw, dw, w), base + (size_t)(d + 1) * cap, lane);
+                if (len[d + 1] > 0) {
+                    idx[d + 1] = 0;
+                    ++d;
+                }
+            }
+        }
+    }
+    if (lane == 0 && acc != 0) add128(out, acc);
+}
+
 // CSR checks: offsets monotone, ids in range, rows strictly increasing, no
 // self loops, every edge present in both directions.
 __global__ void validate_kernel(GraphView g, unsigned* __restrict__ flags) {
@@ -910,6 +1003,53 @@ GPM_API int gpm_tri_count(gpm_graph* g, uint64_t* out) {
     return GPM_OK;
 }
 
+GPM_API int gpm_clique_count(gpm_graph* g, int32_t k, gpm_u128* out) {
+    clear_error();
+    if (!g || !out || k < 3 || k > GPM_MAX_PATTERN) {
+        set_error("gpm_clique_count: need a graph, out and 3 <= k <= %d", GPM_MAX_PATTERN);
+        return GPM_ERR_INVALID_ARG;
+    }
+    int err = 0;
+    DeviceCtx* c = get_ctx(&err);
+    if (!c) return err;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const Options& o = options();
+    const int threads = 256, warps_per_block = threads / 32;
+    const long long blocks = (long long)c->num_sms * 8;
+    const long long warps = blocks * warps_per_block;
+    const size_t per_warp = (size_t)std::max(1, k - 3) * (size_t)std::max(1, g->max_degree);
+    int rc = ensure_scratch(c, warps * per_warp * sizeof(int));
+    if (rc) return rc;
+    DevBuf buf;
+    // cursor, 128-bit count, stripes, stripe
+    GPM_CK(cudaMalloc(&buf.p, 5 * sizeof(unsigned long long)));
+    cudaStream_t st = c->stream;
+    const unsigned long long init[5] = {0, 0, 0, (unsigned long long)std::max<int64_t>(1, o.stripes),
+                                        (unsigned long long)o.stripe};
+    GPM_CK(cudaMemcpyAsync(buf.p, init, sizeof init, cudaMemcpyHostToDevice, st));
+    unsigned long long* d = (unsigned long long*)buf.p;
+    const unsigned long long per_stripe = (g->e_cnt + init[3] - 1) / init[3];
+    const int chunk = (int)std::max<unsigned long long>(1, std::min<unsigned long long>(o.chunk, per_stripe / warps));
+    GPM_CK(cudaEventRecord(c->ev0, st));
+    clique_kernel<<<(unsigned)blocks, threads, 0, st>>>(view_of(g), k, d, d + 1, (int*)c->scratch,
+                                                        (int)std::max<size_t>(1, g->max_degree), chunk, d + 3);
+    GPM_CK(cudaGetLastError());
+    GPM_CK(cudaEventRecord(c->ev1, st));
+    unsigned long long h[2] = {0, 0};
+    GPM_CK(cudaMemcpyAsync(h, d + 1, sizeof h, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    t_ms = ms;
+    t_launches = 1;
+    t_bytes = 0;
+    rc = take_check("gpm_clique_count");
+    if (rc) return rc;
+    out->lo = h[0];
+    out->hi = h[1];
+    return GPM_OK;
+}
+
 GPM_API int gpm_plan_create(const int64_t* tables, int32_t n_words, gpm_plan** out) {
     clear_error();
     if (!out) return GPM_ERR_INVALID_ARG;
@@ -1169,53 +1309,81 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     }
     cudaStream_t st = cudaStreamPerThread;
     // control words: [0] work cursor, [1..2] 128-bit sum, [3..4] stats,
-    // [5..6] stripes/stripe, [7] max degree
+    // [5..6] stripes/stripe, [7] max degree, [8] CSR check flags
     unsigned long long* ctrl = (unsigned long long*)base;
     PairDesc* d_pair = (PairDesc*)(base + 256);
     DevPlan* d_plan = (DevPlan*)(base + 512);
-    int* warp_scratch = (int*)(base + kNoAllocHeader);
-    const unsigned long long init[8] = {0, 0, 0, 0, 0, 1, 0, 0};
+    DonationArea* don = (DonationArea*)(base + kNoAllocHeader);
+    const size_t don_bytes = (sizeof(DonationArea) + 255) & ~(size_t)255;
+    int* warp_scratch = (int*)(base + kNoAllocHeader + don_bytes);
+    const size_t scratch_room = kNoAllocBytes - kNoAllocHeader - don_bytes;
+    uint32_t e_cnt = 0;
+    GPM_CK(cudaMemcpyAsync(&e_cnt, d_rowptr + v_cnt, sizeof e_cnt, cudaMemcpyDeviceToHost, st));
+    GPM_CK(cudaStreamSynchronize(st));
+    // the caller's CSR gets the checks gpm_graph_create applies
+    GraphView view;
+    view.rowptr = d_rowptr;
+    view.col = d_col;
+    view.v_cnt = v_cnt;
+    view.pad_ = 0;
+    view.e_cnt = e_cnt;
+    const unsigned long long init[9] = {0, 0, 0, 0, 0, 1, 0, 0, 0};
     GPM_CK(cudaMemcpyAsync(ctrl, init, sizeof init, cudaMemcpyHostToDevice, st));
     max_degree_kernel<<<sms * 4, 256, 0, st>>>(d_rowptr, v_cnt, (unsigned*)(ctrl + 7));
     GPM_CK(cudaGetLastError());
-    uint32_t e_cnt = 0, maxdeg = 0;
-    GPM_CK(cudaMemcpyAsync(&e_cnt, d_rowptr + v_cnt, sizeof e_cnt, cudaMemcpyDeviceToHost, st));
-    GPM_CK(cudaMemcpyAsync(&maxdeg, ctrl + 7, sizeof maxdeg, cudaMemcpyDeviceToHost, st));
+    validate_kernel<<<sms * 8, 256, 0, st>>>(view, (unsigned*)(ctrl + 8));
+    GPM_CK(cudaGetLastError());
+    unsigned long long got[2] = {0, 0};
+    GPM_CK(cudaMemcpyAsync(got, ctrl + 7, sizeof got, cudaMemcpyDeviceToHost, st));
     GPM_CK(cudaStreamSynchronize(st));
-    // size the grid to what the array holds
+    const unsigned maxdeg = (unsigned)got[0], flags = (unsigned)got[1];
+    if (flags) {
+        set_error("gpm_count_noalloc: malformed CSR (%s%s%s%s%s)", flags & 1 ? "offsets " : "",
+                  flags & 2 ? "ids-out-of-range " : "", flags & 4 ? "self-loops " : "",
+                  flags & 8 ? "unsorted-or-duplicate " : "", flags & 16 ? "asymmetric" : "");
+        return GPM_ERR_INVALID_ARG;
+    }
+    // size the grid to what the array holds and to what is resident at once
+    // (idle warps help with published loops until every warp is done)
     const Options& o = options();
     const int wpb = (int)o.warps_per_block;
+    const int stage_cap = (int)o.stage_max;
+    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
+    GPM_CK(cudaFuncSetAttribute(match_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    GPM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, match_kernel<false, 1>, wpb * 32, smem));
+    if (occ < 1) {
+        set_error("launch shape does not fit an SM: %d warps per block, %zu bytes of shared memory", wpb, smem);
+        return GPM_ERR_INVALID_ARG;
+    }
     const long long cap = std::max<long long>(1, maxdeg);
     const long long per_warp = (long long)hp.nslots * cap;
-    const long long fit = (long long)((kNoAllocBytes - kNoAllocHeader) / ((size_t)per_warp * sizeof(int)));
-    const long long want = (long long)sms * o.blocks_per_sm * wpb;
+    const long long fit = (long long)(scratch_room / ((size_t)per_warp * sizeof(int)));
+    const long long want = (long long)sms * std::min<long long>(o.blocks_per_sm, occ) * wpb;
     const long long warps = std::min(want, fit) / wpb * wpb;
     if (warps < wpb) {
         set_error("gpm_count_noalloc: one block of %d warps needs %lld bytes of scratch (%d sets x largest degree %lld "
                   "x 4 bytes per warp); the allocation-free scratch holds %zu bytes: use gpm_count",
-                  wpb, (long long)wpb * per_warp * 4, hp.nslots, cap, kNoAllocBytes - kNoAllocHeader);
+                  wpb, (long long)wpb * per_warp * 4, hp.nslots, cap, scratch_room);
         return GPM_ERR_UNSUPPORTED;
     }
     PairDesc pd;
-    pd.g.rowptr = d_rowptr;
-    pd.g.col = d_col;
-    pd.g.v_cnt = v_cnt;
-    pd.g.pad_ = 0;
-    pd.g.e_cnt = e_cnt;
+    pd.g = view;
     pd.plan = d_plan;
     pd.ntasks = hp.T == 1 ? (unsigned long long)v_cnt : (unsigned long long)e_cnt;
     pd.cap = (int)cap;
     pd.pad_ = 0;
+    // grabs shrink so that no warp is left without a task (as gpm_count does)
+    const int chunk = (int)std::max<long long>(1, std::min<long long>(o.chunk, (long long)(pd.ntasks / warps)));
     GPM_CK(cudaMemcpyAsync(d_pair, &pd, sizeof pd, cudaMemcpyHostToDevice, st));
     GPM_CK(cudaMemcpyAsync(d_plan, &hp, sizeof hp, cudaMemcpyHostToDevice, st));
+    const int split = (int)o.split;
+    if (split > 0) GPM_CK(cudaMemsetAsync(don, 0, sizeof(DonationArea), st));
     const int alpha4[3] = {(int)o.merge_alpha4[0], (int)o.merge_alpha4[1], (int)o.merge_alpha4[2]};
     GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, st));
-    const int stage_cap = (int)o.stage_max;
-    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
-    GPM_CK(cudaFuncSetAttribute(match_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     match_kernel<false, 1><<<(unsigned)(warps / wpb), wpb * 32, smem, st>>>(
-        d_pair, 1, ctrl, ctrl + 1, warp_scratch, per_warp, (int)o.chunk, ctrl + 5, (int)o.leaf_batch, stage_cap,
-        0, nullptr, 0, nullptr, 0, nullptr, 0, 0, nullptr, 0, 0, ctrl + 3);
+        d_pair, 1, ctrl, ctrl + 1, warp_scratch, per_warp, chunk, ctrl + 5, (int)o.leaf_batch, stage_cap,
+        0, nullptr, 0, split > 0 ? don : nullptr, split, nullptr, 0, 0, nullptr, 0, 0, ctrl + 3);
     GPM_CK(cudaGetLastError());
     unsigned long long raw[2] = {0, 0};
     GPM_CK(cudaMemcpyAsync(raw, ctrl + 1, sizeof raw, cudaMemcpyDeviceToHost, st));

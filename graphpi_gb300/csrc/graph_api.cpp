@@ -85,8 +85,18 @@ gpm_u128 Graph::pattern_matching_u128(const Schedule& schedule) {
     return out;
 }
 
-long long Graph::pattern_matching(const Schedule& schedule, int, bool) {
-    gpm_u128 c = pattern_matching_u128(schedule);
+long long Graph::pattern_matching(const Schedule& schedule, int, bool clique) {
+    gpm_u128 c{0, 0};
+    const int n = schedule.get_size();
+    const int* adj = schedule.get_adj_mat_ptr();
+    bool complete = clique && n >= 3;
+    for (int i = 0; i < n && complete; ++i)
+        for (int j = 0; j < n; ++j)
+            if (i != j && !adj[i * n + j]) complete = false;
+    if (complete)  // the clique fast path: same count, no restriction checks
+        check(gpm_clique_count(device_graph(), n, &c), "Graph::pattern_matching (clique)");
+    else
+        c = pattern_matching_u128(schedule);
     if (c.hi != 0 || c.lo > (uint64_t)LLONG_MAX) {
         fprintf(stderr, "Graph::pattern_matching: count exceeds 2^63-1; use pattern_matching_u128\n");
         return -1;
@@ -103,7 +113,7 @@ long long Graph::pattern_matching_mpi(const Schedule& schedule, int thread_count
 
 namespace {
 
-// Builds the CSR from directed pairs: sort, dedupe, offsets.
+// Builds the CSR from directed pairs on the host: sort, dedupe, offsets.
 void fill_csr(Graph* g, std::vector<std::pair<int, int> >& e) {
     std::sort(e.begin(), e.end());
     e.erase(std::unique(e.begin(), e.end()), e.end());
@@ -177,6 +187,36 @@ void fill_tri_cnt(Graph* g, DataType type) {
 
 }  // namespace
 
+// Builds the CSR on the GPU (gpm_graph_from_edges: symmetrise, sort,
+// deduplicate, offsets on the device; relabelled by degree like every
+// device copy), downloads it in the file's ids into the reference's host
+// fields and keeps the device copy for the counting calls.  Returns
+// false, with nothing changed, when no CUDA device is present; the host
+// builder then does the same steps.
+bool DataLoader::gpu_build_csr(Graph* g, const std::vector<std::pair<int, int> >& e) {
+    std::vector<int32_t> src, dst;
+    src.reserve(e.size() / 2);
+    dst.reserve(e.size() / 2);
+    for (const auto& p : e)
+        if (p.first < p.second) {  // both directions are in e; one is enough
+            src.push_back(p.first);
+            dst.push_back(p.second);
+        }
+    gpm_graph* dev = nullptr;
+    const int rc = gpm_graph_from_edges(g->v_cnt, (int64_t)src.size(), src.data(), dst.data(), 1, &dev);
+    if (rc == GPM_ERR_NO_DEVICE) return false;
+    check(rc, "DataLoader: GPU CSR build");
+    int64_t ecnt = 0, md = 0;
+    check(gpm_graph_stats(dev, nullptr, &ecnt, &md, nullptr), "DataLoader: GPU CSR build");
+    g->e_cnt = (unsigned)ecnt;
+    g->edge = new int[std::max<int64_t>(ecnt, 1)];
+    g->vertex = new unsigned[(size_t)g->v_cnt + 1];
+    check(gpm_graph_download(dev, g->vertex, g->edge), "DataLoader: GPU CSR download");
+    g->max_degree = (int)md;
+    g->dev_ = dev;
+    return true;
+}
+
 bool DataLoader::load_data(Graph*& g, DataType type, const char* path, int oriented_type) {
     if (type == Twitter) return twitter_load_data(g, type, path, oriented_type);
     if (type == Invalid) {
@@ -235,7 +275,7 @@ bool DataLoader::general_load_data(Graph*& g, DataType type, const char* path, i
         for (int i = 0; i < g->v_cnt; ++i) new_id[order[i]] = i;
         for (auto& p : e) p = std::make_pair(new_id[p.first], new_id[p.second]);
     }
-    fill_csr(g, e);
+    if (!gpu_build_csr(g, e)) fill_csr(g, e);
     printf("Success! There are %d nodes and %u edges.\n", g->v_cnt, g->e_cnt);
     fflush(stdout);
     fill_tri_cnt(g, type);

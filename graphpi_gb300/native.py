@@ -6,6 +6,7 @@ import os
 from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgraphpi_gb300.so"
+GEN_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgpm_gen.so"
 
 GPM_OK = 0
 STATUS = {
@@ -49,6 +50,7 @@ SIGNATURES = {
     "gpm_graph_destroy": (I32, [P]),
     "gpm_graph_stats": (I32, [P, PI64, PI64, PI64, PI64]),
     "gpm_tri_count": (I32, [P, PU64]),
+    "gpm_clique_count": (I32, [P, I32, C.POINTER(U128)]),
     "gpm_motifs": (I32, [I32, P, I32, PI32]),
     "gpm_pattern_multiplicity": (I32, [I32, P, PI64]),
     "gpm_schedule_build": (I32, [I32, P, I32, I32, I32, I64, U64, I64, P, I32, PI32, PI32]),
@@ -80,7 +82,12 @@ SIGNATURES = {
     "gpm_mlp_train": (I32, [P, P, P, I32, I32, C.c_float, C.c_float, C.POINTER(C.c_float)]),
 }
 
+GEN_SIGNATURES = {name: SIGNATURES[name] for name in (
+    "gpm_last_error", "gpm_gen_rmat", "gpm_gen_chung_lu", "gpm_csr_from_edges", "gpm_csr_relabel_degree",
+    "gpm_free")}
+
 _lib = None
+_gen_lib = None
 
 
 def lib() -> C.CDLL:
@@ -100,10 +107,30 @@ def lib() -> C.CDLL:
     return _lib
 
 
-def check(code: int, where: str) -> None:
+def gen_lib() -> C.CDLL:
+    """Loads the generator library (include/gpm_gen.h) alone: seeded graphs and
+    host CSR utilities without the engine or the CUDA runtime."""
+    global _gen_lib
+    if _gen_lib is None:
+        if not GEN_LIB_PATH.exists():
+            raise RuntimeError(f"{GEN_LIB_PATH} is missing: build it with `python -m graphpi_gb300.build`")
+        L = C.CDLL(str(GEN_LIB_PATH), mode=os.RTLD_LOCAL if hasattr(os, "RTLD_LOCAL") else 0)
+        for name, (res, args) in GEN_SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _gen_lib = L
+    return _gen_lib
+
+
+def check(code: int, where: str, L: C.CDLL | None = None) -> None:
     if code != GPM_OK:
-        msg = lib().gpm_last_error().decode(errors="replace")
+        msg = (L or lib()).gpm_last_error().decode(errors="replace")
         raise GpmError(code, where, msg)
+
+
+def check_gen(code: int, where: str) -> None:
+    check(code, where, gen_lib())
 
 
 def set_option(key: str, value: int) -> None:

@@ -11,6 +11,10 @@
                   degree uniform in [4, 64], exponent uniform in [2.0, 2.8],
                   seeds 100-355, each paired with one 3-5-vertex motif
     rmat_s24      R-MAT scale 24, seed 4 (6-vertex motifs, learned schedules)
+
+Bounded samples of a job are stripes (the first-level tasks t with
+t mod S == s); random_stripes draws the stripe ids the benchmark and the
+parity tests use.
 """
 from __future__ import annotations
 
@@ -48,6 +52,24 @@ def _unit(seed: int, k: int) -> float:
     x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
     x ^= x >> 31
     return (x >> 11) / float(1 << 53)
+
+
+def random_stripes(stripes: int, count: int, seed: int = 20261204) -> list[int]:
+    """`count` distinct stripe ids in [0, stripes), uniformly drawn from a
+    seeded SplitMix64 stream (the same on every machine and numpy version)."""
+    M = 0xFFFFFFFFFFFFFFFF
+    out, seen, state = [], set(), seed & M
+    while len(out) < min(count, stripes):
+        state = (state + 0x9E3779B97F4A7C15) & M
+        z = state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+        z ^= z >> 31
+        s = ((z >> 11) * stripes) >> 53
+        if s not in seen:
+            seen.add(s)
+            out.append(s)
+    return out
 
 
 def uneven_params(count: int = 256, first_seed: int = 100, n_lo: int = 1000, n_hi: int = 200000):

@@ -102,6 +102,15 @@ GPM_API int gpm_graph_stats(const gpm_graph* g, int64_t* v_cnt, int64_t* e_cnt,
  * model's tri_cnt (src/schedule.cpp:1496). */
 GPM_API int gpm_tri_count(gpm_graph* g, uint64_t* out);
 
+/* k-clique count (3 <= k <= GPM_MAX_PATTERN), the clique fast path: the
+ * count Graph::pattern_matching gives for the complete pattern, computed the
+ * way pattern_matching_func does with clique = true (src/graph.cpp:147-197,
+ * the min_vertex clip of VertexSet::intersection, src/vertex_set.cpp:75-103):
+ * each clique once, as its decreasing vertex sequence, with no restriction
+ * or injectivity checks.  Honours the "stripes"/"stripe" options (the tasks
+ * are the directed edges of the device CSR). */
+GPM_API int gpm_clique_count(gpm_graph* g, int32_t k, gpm_u128* out);
+
 /* ------------------------------------------------------------------ */
 /* pattern, motifs, schedule (host)                                    */
 /* ------------------------------------------------------------------ */
@@ -252,16 +261,22 @@ GPM_API int gpm_mlp_train(gpm_mlp* m, const float* X, const float* T, int32_t n_
  * device synchronisation.
  * The caller passes the CSR already in device memory (layout of
  * gpm_graph_create, counted on the ids as given), schedule tables (host) and
- * the result location (host).  Scratch is a 64 MiB file-scope device array
- * that every GPU loading the library holds until exit; the grid is sized to
- * it, and a pattern/graph whose per-warp sets (scratch sets x largest degree
- * x 4 bytes) do not fit one block returns GPM_ERR_UNSUPPORTED ("use
- * gpm_count").  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  Work runs on the per-thread default stream and the call waits
- * for it.  All calls share the one array: it keeps the last call's contents
- * (each call clears the words that must start at zero), and calls that
- * overlap on the GPU — from several host threads — race on it. */
+ * the result location (host).  The CSR gets the checks gpm_graph_create
+ * applies (GPM_ERR_INVALID_ARG when malformed).  Work runs on the
+ * per-thread default stream, which does not wait for other streams: finish
+ * writing rowptr/col first (synchronize, or wait on an event recorded on
+ * the writing stream).  The call waits for its own work.
+ * Scratch is a 64 MiB file-scope device array that every GPU loading the
+ * library holds until exit; the grid is sized to it (and to the blocks
+ * resident at once), and a pattern/graph whose per-warp sets (scratch sets x
+ * largest degree x 4 bytes) do not fit one block returns
+ * GPM_ERR_UNSUPPORTED ("use gpm_count").  Long loops are shared with idle
+ * warps as in gpm_count ("split"); the pair-sum leaf is off on this path.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: it keeps the last call's contents (each
+ * call clears the words that must start at zero), and calls that overlap on
+ * the GPU — from several host threads — race on it. */
 GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int32_t* d_col,
                               const int64_t* tables, int32_t n_words, gpm_u128* out);
 

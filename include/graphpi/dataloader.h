@@ -3,6 +3,8 @@
 // (include/dataloader.h:28-48 of thu-pacman/GraphPi).
 #pragma once
 #include <map>
+#include <utility>
+#include <vector>
 #include "graph.h"
 
 enum DataType { Patents, Orkut, complete8, LiveJournal, MiCo, Twitter, CiteSeer, Wiki_Vote, Invalid };
@@ -27,5 +29,7 @@ public:
 private:
     bool general_load_data(Graph*& g, DataType type, const char* path, int oriented_type);
     bool twitter_load_data(Graph*& g, DataType type, const char* path, int oriented_type);
+    // CSR of both-direction pairs built on the GPU; false without a device
+    static bool gpu_build_csr(Graph* g, const std::vector<std::pair<int, int> >& e);
     std::map<int, int> id;
 };

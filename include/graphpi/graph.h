@@ -44,5 +44,6 @@ public:
     gpm_graph* device_graph();
 
 private:
+    friend class DataLoader;  // hands over the device CSR it built
     gpm_graph* dev_ = nullptr;
 };

@@ -12,6 +12,15 @@
  *                            has_data (:188-194), unorderd_subtraction_size
  *                            (:196-209).  Sums are 128-bit where the
  *                            reference's long long would overflow.
+ *   oracle_stripes_raw       the same counting split into the GPU engine's
+ *                            first-level tasks (root vertices or directed
+ *                            edges), summed per stripe t mod S == s: the
+ *                            root loop (src/graph.cpp:212-228) and one
+ *                            depth-1 iteration (:366-396) per task
+ *   oracle_pattern_matching_clique
+ *                            the same with the clique function
+ *                            (pattern_matching_func, src/graph.cpp:147-197,
+ *                            clipped intersection src/vertex_set.cpp:75-103)
  *   oracle_triangle_count    Graph::triangle_counting_mt / tc_mt
  *                            (src/graph.cpp:66-95, 112-139)
  *   oracle_brute_force       an independent definition-level count:
@@ -167,7 +176,12 @@ static int bound_at(const ctx_t* c, int depth) {
     return mv;
 }
 
-static void rec(ctx_t* c, int depth) {
+static void rec_range(ctx_t* c, int depth, int lo, int hi);
+static void rec(ctx_t* c, int depth) { rec_range(c, depth, 0, 0x7fffffff); }
+
+/* The recursion at `depth`; a loop level runs only its candidates [lo, hi)
+ * (a part of the loop, so that one long loop can be shared by threads). */
+static void rec_range(ctx_t* c, int depth, int lo, int hi) {
     const sched_t* s = c->s;
     if (c->deadline > 0 && (++c->calls & 1023) == 0 && omp_get_wtime() > c->deadline) c->expired = 1;
     if (c->expired) return;
@@ -211,7 +225,8 @@ static void rec(ctx_t* c, int depth) {
         return;
     }
     int mv = bound_at(c, depth); /* src/graph.cpp:367-396 */
-    for (int i = 0; i < size; ++i) {
+    if (hi > size) hi = size;
+    for (int i = lo; i < hi; ++i) {
         int v = S[i];
         if (mv <= v) break;
         int dup = 0;
@@ -332,6 +347,333 @@ int oracle_pattern_matching_roots_timed(int V, const uint32_t* rp, const int32_t
                                         const int32_t* roots, int64_t nroots, int threads, double seconds,
                                         int64_t* done, uint64_t* raw) {
     return run(V, rp, col, tables, nw, roots, nroots, threads, seconds, done, raw);
+}
+
+/* ---- the clique path ------------------------------------------------------
+ *
+ * Graph::pattern_matching_func with clique = true (src/graph.cpp:147-197):
+ * no restrictions and no injectivity checks; a loop stops at the first
+ * candidate not below the last chosen vertex, every prefix set with a father
+ * keeps only the elements below the vertex just chosen
+ * (VertexSet::intersection's min_vertex clip, src/vertex_set.cpp:75-103),
+ * and the last level adds its loop set's size.  For a clique pattern every
+ * clique is counted once, as its decreasing vertex sequence. */
+static int ctx_alloc(ctx_t* c, const uint32_t* rp, const int32_t* col, int V, int cap);
+static void ctx_free(ctx_t* c);
+
+static int merge_below(const int* a, int na, const int* b, int nb, int lim, int* out) {
+    int i = 0, j = 0, w = 0;
+    while (i < na && j < nb && a[i] < lim && b[j] < lim) {
+        if (a[i] < b[j]) ++i;
+        else if (a[i] > b[j]) ++j;
+        else {
+            out[w++] = a[i];
+            ++i;
+            ++j;
+        }
+    }
+    return w;
+}
+
+static void clique_rec(ctx_t* c, int depth) {
+    const sched_t* s = c->s;
+    const int lsid = s->loop_set[depth];
+    const int* S = c->ptr[lsid];
+    const int size = c->len[lsid];
+    if (size <= 0) return;
+    if (depth == s->n - 1) {
+        c->ans += size;
+        return;
+    }
+    const int last = c->chosen[c->nchosen - 1];
+    for (int i = 0; i < size; ++i) {
+        const int v = S[i];
+        if (last <= v) break;
+        int zero = 0;
+        for (int p = s->last[depth]; p != -1; p = s->next[p]) {
+            const int* nv = c->col + c->rp[v];
+            const int dv = (int)(c->rp[v + 1] - c->rp[v]);
+            const int f = s->father[p];
+            if (f == -1) {
+                c->ptr[p] = nv;
+                c->len[p] = dv;
+            } else {
+                c->len[p] = merge_below(c->ptr[f], c->len[f], nv, dv, v, c->buf[p]);
+                c->ptr[p] = c->buf[p];
+            }
+            if (c->len[p] == 0) {
+                zero = 1;
+                break;
+            }
+        }
+        if (zero) continue;
+        c->chosen[c->nchosen++] = v;
+        clique_rec(c, depth + 1);
+        --c->nchosen;
+    }
+}
+
+/* Graph::pattern_matching's root loop with the clique function, divided by
+ * the redundancy (src/graph.cpp:199-245). */
+int oracle_pattern_matching_clique(int V, const uint32_t* rp, const int32_t* col, const int64_t* tables, int nw,
+                                   int threads, uint64_t* out) {
+    sched_t s;
+    if (parse(tables, nw, &s)) return -1;
+    const int cap = max_isect(V, rp);
+    i128 sum = 0;
+    int bad = 0;
+#pragma omp parallel num_threads(threads > 0 ? threads : omp_get_max_threads()) reduction(| : bad)
+    {
+        ctx_t c;
+        if (ctx_alloc(&c, rp, col, V, cap)) bad = 1;
+        c.s = &s;
+        if (!bad) {
+#pragma omp for schedule(dynamic, 16)
+            for (int v = 0; v < V; ++v) {
+                for (int p = s.last[0]; p != -1; p = s.next[p]) build(&c, p, v);
+                c.nchosen = 0;
+                c.chosen[c.nchosen++] = v;
+                clique_rec(&c, 1);
+            }
+        }
+#pragma omp critical
+        sum += c.ans;
+        ctx_free(&c);
+    }
+    if (bad) return -2;
+    unsigned __int128 q = (unsigned __int128)sum / (unsigned __int128)s.redundancy;
+    out[0] = (uint64_t)q;
+    out[1] = (uint64_t)(q >> 64);
+    return 0;
+}
+
+/* ---- the engine's first-level tasks, stripe by stripe --------------------
+ *
+ * The GPU engine splits a job into first-level tasks: root vertices when the
+ * inclusion–exclusion tail starts at depth 1 (n - k == 1), otherwise the
+ * directed edges e of the CSR, task e = (v0, v1) with v0 the row holding e
+ * and v1 = col[e].  Stripe s of S holds the tasks t with t mod S == s.  This
+ * restates, per task, the reference's root loop (src/graph.cpp:212-228: the
+ * depth-0 prefix sets of v0) and one iteration of the depth-1 loop of
+ * pattern_matching_aggressive_func for the candidate v1 (:366-396:
+ * restriction bound, has_data, prefix sets of depth 1, empty-set skip), then
+ * the recursion from depth 2 (rec above).  A root task is the reference's
+ * root loop body itself.  Sums are the undivided signed 128-bit totals, so
+ * stripes add up to the whole job before the division by the redundancy. */
+static void task_sum(ctx_t* c, int T, int64_t t, int lo, int hi) {
+    const sched_t* s = c->s;
+    int v0, v1 = -1;
+    if (T == 1) {
+        v0 = (int)t;
+    } else {
+        /* last row v with rp[v] <= t */
+        int lo = 0, hi = c->V;
+        while (lo < hi) {
+            int mid = (int)(((int64_t)lo + hi + 1) >> 1);
+            if ((int64_t)c->rp[mid] <= t) lo = mid;
+            else hi = mid - 1;
+        }
+        v0 = lo;
+        v1 = c->col[t];
+    }
+    for (int p = s->last[0]; p != -1; p = s->next[p]) build(c, p, v0);
+    c->nchosen = 0;
+    c->chosen[c->nchosen++] = v0;
+    if (T == 1) {
+        rec(c, 1);
+        return;
+    }
+    if (bound_at(c, 1) <= v1) return;
+    if (v1 == v0) return;
+    for (int p = s->last[1]; p != -1; p = s->next[p]) {
+        build(c, p, v1);
+        if (c->len[p] == 0) return;
+    }
+    c->chosen[c->nchosen++] = v1;
+    rec_range(c, 2, lo, hi);
+}
+
+/* Candidates of the depth-2 loop of task t (0 when depth 2 is not a loop
+ * level or the task ends earlier): the part of the loop set below the
+ * restriction bound. */
+static int depth2_len(ctx_t* c, int T, int64_t t) {
+    const sched_t* s = c->s;
+    if (T < 3 || s->n - 1 <= 2) return 0;
+    int lo = 0, hi = c->V;
+    while (lo < hi) {
+        int mid = (int)(((int64_t)lo + hi + 1) >> 1);
+        if ((int64_t)c->rp[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const int v0 = lo, v1 = c->col[t];
+    for (int p = s->last[0]; p != -1; p = s->next[p]) build(c, p, v0);
+    c->nchosen = 0;
+    c->chosen[c->nchosen++] = v0;
+    if (bound_at(c, 1) <= v1 || v1 == v0) return 0;
+    for (int p = s->last[1]; p != -1; p = s->next[p]) {
+        build(c, p, v1);
+        if (c->len[p] == 0) return 0;
+    }
+    c->chosen[c->nchosen++] = v1;
+    const int sid = s->loop_set[2];
+    return lower_bound_i(c->ptr[sid], c->len[sid], bound_at(c, 2));
+}
+
+/* Per-thread scratch of the stripe counter. */
+static int ctx_alloc(ctx_t* c, const uint32_t* rp, const int32_t* col, int V, int cap) {
+    memset(c, 0, sizeof *c);
+    c->rp = rp;
+    c->col = col;
+    c->V = V;
+    c->cap = cap;
+    int bad = 0;
+    for (int p = 0; p < MAXP; ++p) {
+        c->buf[p] = (int*)malloc(sizeof(int) * (size_t)cap);
+        if (!c->buf[p]) bad = 1;
+    }
+    c->tmp = (int*)malloc(sizeof(int) * (size_t)cap);
+    c->tmp2 = (int*)malloc(sizeof(int) * (size_t)cap);
+    return bad || !c->tmp || !c->tmp2;
+}
+
+static void ctx_free(ctx_t* c) {
+    for (int p = 0; p < MAXP; ++p) free(c->buf[p]);
+    free(c->tmp);
+    free(c->tmp2);
+}
+
+/* Raw sums of n_sched schedules (tables concatenated, nw[i] words each) over
+ * the stripes ids[0, n_ids) of `stripes`: out[2*(i*n_ids + j) ..] = {lo, hi}
+ * of schedule i on stripe ids[j].  All (schedule, task) pairs run in one
+ * dynamically scheduled loop over the host threads; a task whose depth-2 loop
+ * is long is cut into parts of kPart candidates first, so that one heavy
+ * task does not run on one thread alone (the sums are the same: the loop's
+ * total is the sum of its parts). */
+#define kPart 8
+int oracle_stripes_raw(int V, const uint32_t* rp, const int32_t* col, int n_sched, const int64_t* tables,
+                       const int32_t* nw, int64_t stripes, const int64_t* ids, int n_ids, int threads, uint64_t* out) {
+    if (n_sched < 1 || n_ids < 1 || stripes < 1) return -1;
+    const int nth = threads > 0 ? threads : omp_get_max_threads();
+    sched_t* sc = (sched_t*)calloc((size_t)n_sched, sizeof(sched_t));
+    int* Ts = (int*)calloc((size_t)n_sched, sizeof(int));
+    int rc = 0;
+    int64_t off = 0, total = 0;
+    if (!sc || !Ts) rc = -2;
+    for (int i = 0; i < n_sched && !rc; ++i) {
+        if (parse(tables + off, nw[i], &sc[i])) rc = -1;
+        off += nw[i];
+        Ts[i] = sc[i].k ? sc[i].n - sc[i].k : sc[i].n - 1;
+    }
+    for (int j = 0; j < n_ids && !rc; ++j)
+        if (ids[j] < 0 || ids[j] >= stripes) rc = -1;
+    if (rc) {
+        free(sc);
+        free(Ts);
+        return rc;
+    }
+    /* tasks: (output index, task id) */
+    for (int i = 0; i < n_sched; ++i) {
+        const int64_t nt = Ts[i] == 1 ? (int64_t)V : (int64_t)rp[V];
+        for (int j = 0; j < n_ids; ++j)
+            if (ids[j] < nt) total += (nt - ids[j] + stripes - 1) / stripes;
+    }
+    const size_t nt1 = (size_t)(total > 0 ? total : 1);
+    int32_t* ti = (int32_t*)malloc(sizeof(int32_t) * nt1);
+    int64_t* tt = (int64_t*)malloc(sizeof(int64_t) * nt1);
+    int32_t* tl = (int32_t*)malloc(sizeof(int32_t) * nt1); /* depth-2 loop length */
+    int64_t* first = (int64_t*)malloc(sizeof(int64_t) * (nt1 + 1));
+    i128* acc = (i128*)calloc((size_t)n_sched * n_ids, sizeof(i128));
+    if (!ti || !tt || !tl || !first || !acc) rc = -2;
+    if (!rc) {
+        int64_t w = 0;
+        for (int i = 0; i < n_sched; ++i) {
+            const int64_t nt = Ts[i] == 1 ? (int64_t)V : (int64_t)rp[V];
+            for (int j = 0; j < n_ids; ++j)
+                for (int64_t t = ids[j]; t < nt; t += stripes) {
+                    ti[w] = i * n_ids + j;
+                    tt[w] = t;
+                    ++w;
+                }
+        }
+    }
+    const int cap = max_isect(V, rp);
+    int bad = rc != 0;
+    /* phase 1: the length of every task's depth-2 loop */
+    if (!bad) {
+#pragma omp parallel num_threads(nth) reduction(| : bad)
+        {
+            ctx_t c;
+            if (ctx_alloc(&c, rp, col, V, cap)) bad = 1;
+            if (!bad) {
+#pragma omp for schedule(dynamic, 16)
+                for (int64_t x = 0; x < total; ++x) {
+                    const int i = ti[x] / n_ids;
+                    c.s = &sc[i];
+                    tl[x] = depth2_len(&c, Ts[i], tt[x]);
+                }
+            }
+            ctx_free(&c);
+        }
+    }
+    /* work items: task x, candidates [q*kPart, q*kPart + kPart) of its loop */
+    int64_t items = 0;
+    if (!bad) {
+        for (int64_t x = 0; x < total; ++x) {
+            first[x] = items;
+            items += tl[x] > kPart ? (tl[x] + kPart - 1) / kPart : 1;
+        }
+        first[total] = items;
+    }
+    if (!bad) {
+#pragma omp parallel num_threads(nth) reduction(| : bad)
+        {
+            ctx_t c;
+            if (ctx_alloc(&c, rp, col, V, cap)) bad = 1;
+            i128* mine = (i128*)calloc((size_t)n_sched * n_ids, sizeof(i128));
+            if (!mine) bad = 1;
+            if (!bad) {
+                int64_t x = 0;
+#pragma omp for schedule(dynamic, 1)
+                for (int64_t it = 0; it < items; ++it) {
+                    /* the task holding item `it` (items are in task order) */
+                    int64_t a = 0, b = total - 1;
+                    while (a < b) {
+                        int64_t m = (a + b + 1) >> 1;
+                        if (first[m] <= it) a = m;
+                        else b = m - 1;
+                    }
+                    x = a;
+                    const int i = ti[x] / n_ids;
+                    c.s = &sc[i];
+                    c.ans = 0;
+                    int lo = 0, hi = 0x7fffffff;
+                    if (tl[x] > kPart) {
+                        lo = (int)(it - first[x]) * kPart;
+                        hi = lo + kPart;
+                    }
+                    task_sum(&c, Ts[i], tt[x], lo, hi);
+                    mine[ti[x]] += c.ans;
+                }
+#pragma omp critical
+                for (int q = 0; q < n_sched * n_ids; ++q) acc[q] += mine[q];
+            }
+            free(mine);
+            ctx_free(&c);
+        }
+    }
+    if (!bad)
+        for (int q = 0; q < n_sched * n_ids; ++q) {
+            out[2 * q] = (uint64_t)acc[q];
+            out[2 * q + 1] = (uint64_t)(acc[q] >> 64);
+        }
+    free(sc);
+    free(Ts);
+    free(ti);
+    free(tt);
+    free(tl);
+    free(first);
+    free(acc);
+    return bad ? (rc ? rc : -2) : 0;
 }
 
 long long oracle_triangle_count(int V, const uint32_t* rp, const int32_t* col, int threads) {

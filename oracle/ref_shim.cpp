@@ -15,7 +15,21 @@
 //   ref_schedule_dump       -> the schedule getters (include/schedule.h:23-37)
 //   ref_motifs              -> MotifGenerator::generate (src/motif_generator.cpp:33-43)
 //   ref_load_data           -> DataLoader::load_data (src/dataloader.cpp:8-163)
+//   ref_stripes_raw         -> the counting of Graph::pattern_matching split
+//                              into first-level tasks (root vertices, or the
+//                              directed edges (v0, v1) of the CSR) and summed
+//                              per stripe t mod S == s; each task runs the
+//                              reference's own root-loop body
+//                              (src/graph.cpp:212-228), one depth-1 loop
+//                              iteration (:366-396) and
+//                              pattern_matching_aggressive_func from depth 2
+//
+// The depth-level function is private to Graph (include/graph.h:50-55); this
+// test-only translation unit opens the class so that it can call it.  The
+// reference's own objects are compiled unchanged.
+#define private public
 #include "graph.h"
+#undef private
 #include "dataloader.h"
 #include "pattern.h"
 #include "schedule.h"
@@ -145,6 +159,84 @@ void* ref_load_data(const char* path, int data_type, int oriented_type) {
     Graph* g = nullptr;
     if (!D.load_data(g, (DataType)data_type, path, oriented_type)) return nullptr;
     return g;
+}
+
+// Raw (undivided) sums of one schedule over the stripes ids[0, n_ids) of
+// `stripes`: out[j] = sum over the tasks t of stripe ids[j].  The tasks of
+// all stripes share one dynamically scheduled loop.  Sums are the
+// reference's long long; where they exceed 64 bits they wrap, so callers
+// compare them modulo 2^64.
+int ref_stripes_raw(void* gp, void* sp, long long stripes, const long long* ids, int n_ids, int threads,
+                    long long* out) {
+    Graph* g = (Graph*)gp;
+    const Schedule& s = *(Schedule*)sp;
+    const int n = s.get_size(), k = s.get_in_exclusion_optimize_num();
+    const int T = k ? n - k : n - 1;
+    const long long nt = T == 1 ? (long long)g->v_cnt : (long long)g->e_cnt;
+    std::vector<long long> task;
+    std::vector<int> owner;
+    for (int j = 0; j < n_ids; ++j)
+        for (long long t = ids[j]; t < nt; t += stripes) {
+            task.push_back(t);
+            owner.push_back(j);
+        }
+    std::vector<long long> sums(n_ids, 0);
+#pragma omp parallel num_threads(threads)
+    {
+        VertexSet* vertex_set = new VertexSet[s.get_total_prefix_num()];
+        VertexSet subtraction_set;
+        VertexSet tmp_set;
+        subtraction_set.init();
+        std::vector<long long> mine(n_ids, 0);
+#pragma omp for schedule(dynamic)
+        for (long long x = 0; x < (long long)task.size(); ++x) {
+            const long long t = task[x];
+            long long local_ans = 0;
+            int v0, v1 = -1;
+            if (T == 1) {
+                v0 = (int)t;
+            } else {
+                v0 = (int)(std::upper_bound(g->vertex, g->vertex + g->v_cnt + 1, (unsigned)t) - g->vertex) - 1;
+                v1 = g->edge[t];
+            }
+            unsigned l, r;
+            g->get_edge_index(v0, l, r);
+            for (int p = s.get_last(0); p != -1; p = s.get_next(p))
+                vertex_set[p].build_vertex_set(s, vertex_set, &g->edge[l], (int)r - l, p);
+            subtraction_set.push_back(v0);
+            if (T == 1) {
+                g->pattern_matching_aggressive_func(s, vertex_set, subtraction_set, tmp_set, local_ans, 1);
+            } else {
+                int min_vertex = g->v_cnt;
+                for (int i = s.get_restrict_last(1); i != -1; i = s.get_restrict_next(i))
+                    if (min_vertex > subtraction_set.get_data(s.get_restrict_index(i)))
+                        min_vertex = subtraction_set.get_data(s.get_restrict_index(i));
+                if (min_vertex > v1 && !subtraction_set.has_data(v1)) {
+                    g->get_edge_index(v1, l, r);
+                    bool is_zero = false;
+                    for (int p = s.get_last(1); p != -1; p = s.get_next(p)) {
+                        vertex_set[p].build_vertex_set(s, vertex_set, &g->edge[l], (int)r - l, p, v1);
+                        if (vertex_set[p].get_size() == 0) {
+                            is_zero = true;
+                            break;
+                        }
+                    }
+                    if (!is_zero) {
+                        subtraction_set.push_back(v1);
+                        g->pattern_matching_aggressive_func(s, vertex_set, subtraction_set, tmp_set, local_ans, 2);
+                        subtraction_set.pop_back();
+                    }
+                }
+            }
+            subtraction_set.pop_back();
+            mine[owner[x]] += local_ans;
+        }
+#pragma omp critical
+        for (int j = 0; j < n_ids; ++j) sums[j] += mine[j];
+        delete[] vertex_set;
+    }
+    for (int j = 0; j < n_ids; ++j) out[j] = sums[j];
+    return 0;
 }
 
 }  // extern "C"

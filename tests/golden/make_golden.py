@@ -1,8 +1,8 @@
 """Generates the golden fixtures in this folder from the reference GraphPi
 itself (oracle/_ref/libgraphpi_ref.so, built from the reference sources by
-oracle/build_ref.sh).  Run where the reference checkout exists:
+oracle/build_ref.sh).  Run where the reference checkout exists, naming it:
 
-    python tests/golden/make_golden.py
+    GRAPHPI_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 
 Writes
   schedules.json  reference Schedule tables (gpm_schedule_build layout) for
@@ -19,6 +19,7 @@ from __future__ import annotations
 import ctypes as C
 import hashlib
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -31,7 +32,9 @@ import graphpi_gb300 as gp  # noqa: E402
 from graphpi_gb300 import workloads  # noqa: E402
 
 REF = ROOT / "oracle" / "_ref" / "libgraphpi_ref.so"
-WIKI = Path("/root/reference/dataset/wiki-vote_input")
+if not os.environ.get("GRAPHPI_REFERENCE"):
+    sys.exit("set GRAPHPI_REFERENCE to the reference checkout")
+WIKI = Path(os.environ["GRAPHPI_REFERENCE"]) / "dataset" / "wiki-vote_input"
 OUT = Path(__file__).resolve().parent
 
 

@@ -29,6 +29,20 @@ def test_every_declared_symbol_is_exported(engine):
         assert s in native.SIGNATURES, f"{s} has no Python binding"
 
 
+def test_generator_library_stands_alone():
+    """libgpm_gen.so exports every gpm_gen.h entry point and loads without
+    the engine (the CPU reference arm generates its graphs with it)."""
+    names = [m.group(1) for m in re.finditer(r"GPM_API\s+[\w\s\*]+?\b(gpm_\w+)\s*\(",
+                                             (INCLUDE / "gpm_gen.h").read_text())]
+    L = native.gen_lib()
+    for s in names:
+        assert hasattr(L, s), s
+    g = gp.rmat(8, 8, 0.57, 0.19, 0.19, 1)
+    h = gp.relabel_by_degree(g)
+    assert h.e_cnt == g.e_cnt and sorted(np.diff(h.vertex.astype(np.int64)).tolist(), reverse=True) == \
+        np.diff(h.vertex.astype(np.int64)).tolist()
+
+
 def test_plan_rejects_bad_tables(engine):
     bad = np.array([3, 0, 1], dtype=np.int64)
     h = C.c_void_p()

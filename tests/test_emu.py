@@ -20,7 +20,7 @@ CSRC = ROOT / "graphpi_gb300" / "csrc"
 EMU = ROOT / "tests" / "emu"
 OUT = ROOT / "graphpi_gb300" / "_build" / "emu"
 
-HOST_SOURCES = ["capi_host.cpp", "schedule.cpp", "pattern.cpp", "gen.cpp"]
+HOST_SOURCES = ["capi_host.cpp", "errors.cpp", "schedule.cpp", "pattern.cpp", "gen.cpp"]
 FLAGS = ["-O1", "-g", "-fsanitize=address", "-fno-omit-frame-pointer", "-fopenmp", "-ffp-contract=off"]
 INCLUDES = [f"-I{ROOT / 'include'}", f"-I{CSRC}", f"-I{EMU}"]
 

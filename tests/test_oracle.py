@@ -9,10 +9,11 @@ import pytest
 
 import graphpi_gb300 as gp
 from graphpi_gb300 import workloads
-from tests.oracle_lib import REF_LIB, csr_checksum, golden
+from tests.oracle_lib import REF_LIB, csr_checksum, golden, reference_root
 
 COUNTS = golden("counts.json")
-WIKI = Path("/root/reference/dataset/wiki-vote_input")
+_REF = reference_root()
+WIKI = _REF / "dataset" / "wiki-vote_input" if _REF else None
 
 GEN = {
     "chung_lu_7k": workloads.chung_lu_7k,
@@ -105,7 +106,8 @@ def test_oracle_matches_live_reference(engine, oracle):
     R.ref_graph_free(rg)
 
 
-@pytest.mark.skipif(not WIKI.exists(), reason="Wiki-Vote dataset only in the reference checkout")
+@pytest.mark.skipif(WIKI is None or not WIKI.exists(),
+                    reason="Wiki-Vote dataset: set GRAPHPI_REFERENCE to the reference checkout")
 def test_oracle_wiki_vote(engine, oracle):
     g = gp.DataLoader().load_data(gp.DataType.Wiki_Vote, str(WIKI))
     w = COUNTS["wiki_vote"]
@@ -114,3 +116,66 @@ def test_oracle_wiki_vote(engine, oracle):
     for name, p in [("rectangle", gp.Pattern(gp.PatternType.Rectangle)), ("clique4", gp.Pattern(4, True))]:
         s = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, g.tri_cnt)
         assert oracle.count(g, s) == w[name]
+
+
+def test_oracle_stripes_sum_to_whole_job(engine, oracle):
+    """The engine's first-level task split: stripes of every size add up to
+    the whole job's undivided sum, for edge-task and root-task plans."""
+    g = gp.relabel_by_degree(gp.rmat(10, 12, 0.57, 0.19, 0.19, 4))
+    tri = oracle.triangles(g)
+    pats = gp.motifs_3_to_5()
+    scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in pats]
+    for S in (1, 5, 64):
+        sums = oracle.stripes_raw(g, [s.tables for s in scheds], S, list(range(S)))
+        for s, row in zip(scheds, sums):
+            assert sum(row) // s.get_in_exclusion_optimize_redundancy() == oracle.count(g, s)
+
+
+@pytest.mark.skipif(not REF_LIB.exists(), reason="reference library not built here")
+def test_oracle_stripes_match_live_reference(engine, oracle):
+    """Per-stripe sums of the oracle equal the reference's own code run on
+    the same task split (ref_stripes_raw), on all 29 motifs."""
+    from tests import oracle_lib
+    R = oracle_lib.load_ref()
+    g = gp.relabel_by_degree(gp.rmat(11, 8, 0.57, 0.19, 0.19, 9))
+    tri = oracle.triangles(g)
+    rg = R.ref_graph_from_csr(g.v_cnt, g.vertex.ctypes.data, g.edge.ctypes.data, -1, 4)
+    S, ids = 7, np.arange(7, dtype=np.int64)
+    for p in gp.motifs_3_to_5():
+        tabs, ok = oracle_lib.ref_schedule_tables(R, p.adj, 1, 1, True, g.v_cnt, g.e_cnt, tri)
+        a = np.ascontiguousarray(p.adj, dtype=np.int32)
+        okc = C.c_int()
+        rs = R.ref_schedule_create(a.shape[0], a.ctypes.data, 1, 1, 1, g.v_cnt, g.e_cnt, tri, C.byref(okc))
+        ref = np.zeros(S, dtype=np.int64)
+        R.ref_stripes_raw(rg, rs, S, ids.ctypes.data, S, 4, ref.ctypes.data)
+        R.ref_schedule_free(rs)
+        assert oracle.stripes_raw(g, [tabs], S, ids)[0] == ref.tolist(), p
+    R.ref_graph_free(rg)
+
+
+def test_bench_golden_records_reference_tables():
+    """The recorded benchmark fixture names its graphs and its stripe ids
+    are the seeded ones the benchmark draws."""
+    import json
+    e = json.loads((Path(__file__).resolve().parent / "golden" / "bench_stripes.json").read_text())
+    for name, scale in (("rmat_s22", 22), ("rmat_s20", 20)):
+        x = e[name]
+        assert x["scale"] == scale and x["flags"] == [1, 1, 1]
+        assert x["ids"] == workloads.random_stripes(x["stripes"], len(x["ids"]))
+        assert len(x["tables"]) == len(x["raw"]) == len(x["names"])
+        assert all(len(r) == len(x["ids"]) for r in x["raw"])
+
+
+def test_oracle_clique_path_counts_cliques(engine, oracle):
+    """The reference's clique function (pattern_matching_func, clique = true)
+    counts each k-clique once: it equals the general path and the brute
+    force for complete patterns."""
+    for g in (gp.chung_lu(300, 14.0, 2.2, 80, 3), gp.rmat(9, 12, 0.57, 0.19, 0.19, 2)):
+        tri = oracle.triangles(g)
+        for k in (3, 4, 5, 6):
+            s = gp.Schedule(gp.Pattern(k, True), 1, 1, True, g.v_cnt, g.e_cnt, tri)
+            assert s.is_complete()
+            want = oracle.count(g, s)
+            assert oracle.count_clique(g, s) == want, k
+            if k <= 5:
+                assert oracle.brute_force(g, gp.Pattern(k, True)) == want, k

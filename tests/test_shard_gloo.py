@@ -1,6 +1,7 @@
 """The multi-rank split on CPU: two gloo ranks each count their interleaved
-share of the roots with the oracle, the raw 128-bit sums are reduced exactly,
-and the result equals the single-process count."""
+share of the engine's first-level tasks (stripes t mod S, restated by the
+oracle), the raw 128-bit sums are reduced exactly, and the result equals the
+single-process count."""
 import os
 import socket
 
@@ -28,13 +29,13 @@ def _rank(rank, world, port, q):
     tri = orc.triangles(g, 1)
     pats = [gp.Pattern(gp.PatternType.House), gp.Pattern(gp.PatternType.Rectangle), gp.Pattern(4, True)]
     scheds = [gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in pats]
+    # the engine's task split (directed edges of the degree-relabelled CSR,
+    # or roots), restated by the oracle: rank r takes stripes r, r + N, ...
+    g = gp.relabel_by_degree(g)
     stripes = 8
-    raws = []
-    for s in scheds:
-        tot = 0
-        for st in shard.stripes_of_rank(rank, world, stripes):
-            tot += orc.raw_roots(g, s, np.arange(st, g.v_cnt, stripes), 1)
-        raws.append(tot)
+    mine = shard.stripes_of_rank(rank, world, stripes)
+    per = orc.stripes_raw(g, [s.tables for s in scheds], stripes, mine, 1)
+    raws = [sum(row) for row in per]
     totals = shard.reduce_raw_sums(raws, dist)
     counts = shard.finish(totals, [s.get_in_exclusion_optimize_redundancy() for s in scheds])
     if rank == 0:

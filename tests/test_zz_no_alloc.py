@@ -45,6 +45,37 @@ def test_noalloc_matches_gpm_count_twice(engine):
             assert _noalloc(g, s) == want
 
 
+def test_noalloc_hub_cut_grid_matches_oracle(engine, oracle):
+    """A hub of degree 19,999: one warp's sets need about 320 KB, so the grid
+    is cut to the warps the fixed array holds (far fewer than a full grid)
+    and long loops are shared with idle warps; counts equal the oracle's."""
+    rng = np.random.default_rng(5)
+    n = 20000
+    src = np.concatenate([np.zeros(n - 1, dtype=np.int32), rng.integers(1, n, 60000, dtype=np.int32)])
+    dst = np.concatenate([np.arange(1, n, dtype=np.int32), rng.integers(1, n, 60000, dtype=np.int32)])
+    g = gp.from_edges(n, src, dst)
+    tri = oracle.triangles(g)
+    for p in (gp.Pattern(gp.PatternType.House), gp.Pattern(gp.PatternType.Rectangle)):
+        s = gp.Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri)
+        want = oracle.count(g, s)
+        assert _noalloc(g, s) == want
+        assert _noalloc(g, s) == want
+
+
+def test_noalloc_rejects_malformed_csr(engine):
+    """The caller's CSR is checked like gpm_graph_create's: a one-way edge and
+    an unsorted list are invalid arguments, not silently wrong counts."""
+    s = gp.Schedule(gp.Pattern(3, True), 0, 0, False, 3, 2, 0)
+    for rowptr, col in (([0, 1, 1, 1], [1]), ([0, 2, 3, 4], [2, 1, 0, 0])):
+        rp = torch.tensor(rowptr, dtype=torch.int32, device="cuda")
+        cl = torch.tensor(col, dtype=torch.int32, device="cuda")
+        torch.cuda.synchronize()
+        t = np.ascontiguousarray(s.tables, dtype=np.int64)
+        out = native.U128()
+        rc = gp.lib().gpm_count_noalloc(3, rp.data_ptr(), cl.data_ptr(), t.ctypes.data, len(t), C.byref(out))
+        assert rc == 1, gp.lib().gpm_last_error()
+
+
 def test_noalloc_rejects_oversized(engine):
     # one hub of degree 2,000,000: a warp's sets cannot fit the fixed scratch
     d = 2_000_000
