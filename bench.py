@@ -319,6 +319,24 @@ def run_ours(args, rank: int, world: int) -> dict | None:
                 by_pattern[j].append(m)
         print(f"[bench] plain: {[round(x, 1) for x in plain_ms]}", file=sys.stderr, flush=True)
 
+    # ---- per-schedule generated kernels, one launch pair per pattern -------
+    gen_ms, gen_by_pattern, gen_compile_s = [], [[] for _ in plans], None
+    if args.generated:
+        from graphpi_gb300 import codegen
+        t = time.time()
+        gen = codegen.Generated(scheds)
+        gen_compile_s = time.time() - t
+        for s, want in zip(timed_ids, raws_all):
+            tot = 0.0
+            for j in range(n):
+                r = gen.raw(g, j, stripes=S, stripe=s)
+                if r != want[j]:
+                    raise AssertionError(f"stripe {s}, pattern {j}: generated kernel and interpreter differ")
+                tot += gen.last_ms
+                gen_by_pattern[j].append(gen.last_ms)
+            gen_ms.append(tot)
+        print(f"[bench] generated: {[round(x, 1) for x in gen_ms]}", file=sys.stderr, flush=True)
+
     # ---- algorithmic bytes of one launch (separate counting run) ----------
     gp.set_option("count_bytes", 1)
     algo_bytes = 0
@@ -411,6 +429,13 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "cpu_baseline": cpu,
         "setup_s": {"generate": round(gen_s, 2), "upload_relabel": round(upload_s, 3)},
     }
+    if gen_ms:
+        res["generated"] = {
+            "what": "per-schedule generated kernels (graphpi_gb300/codegen.py), one pattern per launch, same stripes",
+            "ms_per_step": statistics.median(gen_ms), "ms_by_motif": [round(sum(m), 2) for m in gen_by_pattern],
+            "compile_s": round(gen_compile_s, 1),
+            "vs_interpreted_one_pattern_per_launch": (statistics.median(plain_ms) / statistics.median(gen_ms)
+                                                      if plain_ms else None)}
     if cfg["batched"]:
         res["plain_per_pattern_ms_per_step"] = statistics.median(plain_ms)
         res["plain_ms_by_motif"] = [round(sum(m), 2) for m in by_pattern]
@@ -520,6 +545,8 @@ def main() -> None:
     ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
     ap.add_argument("--stripes", type=int, default=0, help="stripes per full job (0: the config's)")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--generated", type=int, default=1, choices=[0, 1],
+                    help="also time the per-schedule generated kernels on the same stripes")
     ap.add_argument("--pair-max-ops", type=int, default=None,
                     help="longest pair sum one warp takes on (default: the engine's)")
     ap.add_argument("--leaf-batch", type=int, default=None, choices=[0, 1],

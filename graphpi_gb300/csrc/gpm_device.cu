@@ -941,6 +941,19 @@ GPM_API int gpm_graph_download(const gpm_graph* g, uint32_t* rowptr, int32_t* co
     return GPM_OK;
 }
 
+GPM_API int gpm_graph_device_csr(const gpm_graph* g, int32_t caller_ids, const uint32_t** rowptr,
+                                 const int32_t** col) {
+    clear_error();
+    if (!g || !rowptr || !col) {
+        set_error("gpm_graph_device_csr: null argument");
+        return GPM_ERR_INVALID_ARG;
+    }
+    const GraphView v = view_of(g, caller_ids != 0);
+    *rowptr = v.rowptr;
+    *col = v.col;
+    return GPM_OK;
+}
+
 GPM_API int gpm_graph_destroy(gpm_graph* g) {
     clear_error();
     if (!g) return GPM_OK;

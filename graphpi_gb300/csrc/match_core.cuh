@@ -74,13 +74,22 @@ struct WarpState {
 constexpr int kDonSlots = 1024;
 constexpr int kErrDonation = 4;
 
+// Record kinds: a loop of depth d, the batched deepest level (taken in
+// coarser slices), and the two phases of a shared pair sum: filling the
+// owner's table from the smaller side's candidates, then probing it with the
+// other side's (the owner waits until every slice of a phase is done).
+constexpr int kDonLoop = 0, kDonLeaf = 1, kDonPairFill = 2, kDonPairProbe = 3;
+constexpr int kDonSideA = 0x100;  // pair-sum phases: the phase runs over side A (level L-1)
+
 struct Donation {
     unsigned long long word;  // generation (16 bits) | end (24) | next (24)
     int pair;
     int depth;
     int chosen[kMaxN];
-    int leaf;  // 1: the batched deepest level, taken in coarser slices
-    int pad_[3];
+    int kind;        // kDon*
+    int owner;       // pair sums: global warp index of the table's owner
+    unsigned epoch;  // pair sums: tag of the owner's live table entries
+    unsigned done;   // pair sums: candidates of the phase finished
 };
 static_assert(sizeof(Donation) == 64, "one record per 64 bytes");
 
@@ -98,18 +107,22 @@ __device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned en
 
 // Takes the next slice of record r (generation gen); lo == hi when the loop
 // is exhausted or the slot holds another generation.  A slice is 1/32 of
-// what is left, within [1, 64] candidates of a loop or [8, 128] of a
-// batched leaf level.  Lock-free: a failed compare-and-swap means another
+// what is left, within the bounds of the record's kind.  Lock-free: a failed compare-and-swap means another
 // warp took a slice, so the retries are bounded by the loop length (< 2^24).
-__device__ void don_claim(Donation* r, unsigned gen, bool leaf, int& lo, int& hi) {
+__device__ void don_claim(Donation* r, unsigned gen, int kind, int& lo, int& hi) {
     lo = hi = 0;
     unsigned long long w = *(volatile unsigned long long*)&r->word;
+    // slice bounds per kind: loops [1, 64], batched leaves [8, 128], pair-sum
+    // phases [1, 16] candidates (each carries a whole neighbour list)
+    kind &= 0xff;
+    const unsigned smin = kind == kDonLeaf ? 8u : 1u;
+    const unsigned smax = kind == kDonLeaf ? 128u : (kind == kDonLoop ? 64u : 16u);
     for (int tries = 0; tries < (1 << 25); ++tries) {
         if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
         const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
         if (next >= end) return;
         const unsigned want = (end - next) >> 5;
-        const unsigned take = min(end - next, leaf ? min(128u, max(8u, want)) : min(64u, max(1u, want)));
+        const unsigned take = min(end - next, min(smax, max(smin, want)));
         const unsigned long long got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
         if (got == w) {
             lo = (int)next;
@@ -346,6 +359,8 @@ struct WarpCtx {
     int stage_cap;
     int pair_on;
     unsigned long long* ptab;  // this warp's pair-sum table (pmask + 1 words)
+    unsigned long long* ptab_base;  // every warp's tables, 2^pair_log2 words each
+    int pair_log2;
     unsigned pmask;
     DonationArea* don;         // null: no donation
     int split_min;             // smallest loop that is donated
@@ -520,42 +535,175 @@ struct WarpCtx {
         return true;
     }
 
+    // The two sides of the pair sum of level L-1 (whose loop list is set):
+    // the level L-1 candidates A, the level L candidates B (below their
+    // bound; neither depends on v_{L-1}) and the tail's bound.
+    __device__ void pair_sides(const int*& candA, int& na, const int*& candB, int& nb, int& bnd) {
+        const int L1 = P->L - 1;
+        candA = s->lp[L1];
+        na = s->end[L1];
+        const int sb = P->loop_set[P->L];
+        candB = s->ptr[sb];
+        nb = lower_bound_u(candB, s->len[sb], bound_of(P->L));
+        bnd = bound_of(P->T);
+    }
+
+    // Σ over the candidates not chosen before L-1 of |N(w) ∩ [0, bnd)| (warp-uniform)
+    __device__ long long side_total(const int* cand, int nc, int bnd) {
+        const int L1 = P->L - 1;
+        long long m = 0;
+        for (int base = 0; base < nc; base += 32) {
+            const int j = base + lane;
+            int len = 0;
+            if (j < nc) {
+                const int w = cand[j];
+                if (!chosen_before(w, L1)) {
+                    const unsigned st = g.rowptr[w];
+                    len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
+                }
+            }
+            int pre;
+            m += warp_scan(len, pre);
+        }
+        return m;
+    }
+
+    // One pass over the neighbour lists of cand[lo, hi) below bnd, for each
+    // element x not chosen before L-1: phase 0 adds one to x's count in table
+    // T (tag ep), phase 1 sums the counts (returns this lane's share).
+    __device__ long long pair_pass(const int* cand, int lo, int hi, int bnd, unsigned long long* T, unsigned ep,
+                                   int phase) {
+        const int L1 = P->L - 1;
+        long long sum = 0;
+        for (int base = lo; base < hi; base += 32) {
+            const int j = base + lane;
+            unsigned st = 0;
+            int len = 0;
+            if (j < hi) {
+                const int v = cand[j];
+                if (!chosen_before(v, L1)) {
+                    st = g.rowptr[v];
+                    len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
+                    if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
+                }
+            }
+            int pre;
+            const int M = warp_scan(len, pre);
+            for (int eb = 0; eb < M; eb += 32) {
+                const int e = eb + lane;
+                const int c = owner(pre, e);
+                const unsigned stc = __shfl_sync(kFull, st, c);
+                const int prc = __shfl_sync(kFull, pre, c);
+                if (e < M) {
+                    const int x = g.col[stc + (e - prc)];
+                    if (!chosen_before(x, L1)) {
+                        if (phase == 0) {
+                            if (!pair_add(T, pmask, ep, x)) record_check(3, x, hi - lo, pmask, 0, 0, 0);
+                        } else {
+                            sum += pair_get(T, pmask, ep, x);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        return sum;
+    }
+
+    // Publishes one phase of a shared pair sum in slot h (held by this warp):
+    // n candidates, a new generation; returns the generation (lane 0's value
+    // on every lane).
+    __device__ unsigned pair_publish(int h, int kind, int n, unsigned ep) {
+        unsigned gen = 0;
+        __syncwarp();
+        if (lane == 0) {
+            Donation* r = &don->rec[h];
+            volatile Donation* vr = r;
+            gen = ((unsigned)(vr->word >> 48) + 1u) & 0xffffu;
+            vr->pair = pair_idx;
+            vr->depth = P->L - 1;
+            vr->kind = kind;
+            vr->owner = (int)gw;
+            vr->epoch = ep;
+            vr->done = 0u;
+            for (int j = 0; j < P->L - 1; ++j) vr->chosen[j] = s->chosen[j];
+            __threadfence();
+            atomicExch(&r->word, don_pack(gen, (unsigned)n, 0u));
+        }
+        return __shfl_sync(kFull, gen, 0);
+    }
+
+    // Takes slices of one pair-sum phase (record h, generation gen) over
+    // cand until none is left; every finished slice is added to the
+    // record's done count.  Returns this lane's share of the probe sums.
+    __device__ long long pair_slices(int h, unsigned gen, int kind, const int* cand, int bnd,
+                                     unsigned long long* T, unsigned ep) {
+        Donation* r = &don->rec[h];
+        long long sum = 0;
+        for (;;) {
+            int lo = 0, hi = 0;
+            if (lane == 0) don_claim(r, gen, kind, lo, hi);
+            lo = __shfl_sync(kFull, lo, 0);
+            hi = __shfl_sync(kFull, hi, 0);
+            if (hi <= lo) break;
+            sum += pair_pass(cand, lo, hi, bnd, T, ep, (kind & 0xff) == kDonPairFill ? 0 : 1);
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();  // the slice's table updates before its count
+                atomicAdd(&r->done, (unsigned)(hi - lo));
+            }
+        }
+        return sum;
+    }
+
+    // Waits until every slice of the phase in record h is finished (the
+    // helpers holding slices are running, so the wait ends); bounded, and
+    // recorded as a check failure if the bound is reached.
+    __device__ bool pair_wait(int h, int n) {
+        unsigned d = 0;
+        for (int it = 0; it < (1 << 24); ++it) {
+            if (lane == 0) d = atomicAdd(&don->rec[h].done, 0u);
+            d = __shfl_sync(kFull, d, 0);
+            if (d >= (unsigned)n) {
+                __threadfence();
+                return true;
+            }
+            __nanosleep(256);
+        }
+        if (lane == 0) record_check(kErrDonation, h, n, d, 0, 0, 2);
+        return false;
+    }
+
+    // A free donation slot for this warp, or -1 (lane 0 searches).
+    __device__ int take_slot(int salt) {
+        int h = -1;
+        if (lane == 0) {
+            for (int probe = 0; probe < 4 && h < 0; ++probe) {
+                const int c = (int)((gw * 7 + salt * 131 + probe * 257) & (kDonSlots - 1));
+                if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
+            }
+        }
+        return __shfl_sync(kFull, h, 0);
+    }
+
     // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
     // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
     // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
     // (and does nothing) when the smaller side's neighbour lists would fill
     // the table more than half: the caller then runs the level normally.
+    // A long pair sum is shared: idle warps take slices of the fill phase
+    // (inserting into this warp's table) and then of the probe phase (adding
+    // their sums to the pair's result), so one warp no longer carries a hub
+    // pair sum alone.
     __device__ bool pair_level(__int128& out) {
         const int L1 = P->L - 1;
-        const int T = P->T;
-        const int* candA = s->lp[L1];
-        const int na = s->end[L1];
-        const int sb = P->loop_set[P->L];
-        const int* candB = s->ptr[sb];
-        const int nb = lower_bound_u(candB, s->len[sb], bound_of(P->L));
-        const int bnd = bound_of(T);
+        const int* candA;
+        const int* candB;
+        int na, nb, bnd;
+        pair_sides(candA, na, candB, nb, bnd);
         // sizes of A's and B's neighbour lists below the bound; the smaller
         // side fills the table, the other probes it (the sum is symmetric)
-        long long ma = 0, mb = 0;
-        for (int side = 0; side < 2; ++side) {
-            const int* cand = side == 0 ? candA : candB;
-            const int nc = side == 0 ? na : nb;
-            long long m = 0;
-            for (int base = 0; base < nc; base += 32) {
-                const int j = base + lane;
-                int len = 0;
-                if (j < nc) {
-                    const int w = cand[j];
-                    if (!chosen_before(w, L1)) {
-                        const unsigned st = g.rowptr[w];
-                        len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
-                    }
-                }
-                int pre;
-                m += warp_scan(len, pre);
-            }
-            (side == 0 ? ma : mb) = m;
-        }
+        const long long ma = side_total(candA, na, bnd), mb = side_total(candB, nb, bnd);
         if (c_pair_max_ops > 0 && ma + mb > c_pair_max_ops) return false;
         const long long mins = min(ma, mb);
         const bool a_fills = ma < mb;
@@ -571,44 +719,32 @@ struct WarpCtx {
             for (unsigned i = lane; i <= pmask; i += 32) ptab[i] = 0ull;
             __syncwarp();
         }
+        const int* fill = a_fills ? candA : candB;
+        const int nfill = a_fills ? na : nb;
+        const int* probe = a_fills ? candB : candA;
+        const int nprobe = a_fills ? nb : na;
         long long sum = 0;
-        // phase 0 (smaller side -> counts) and phase 1 (other side -> sum of counts)
-        for (int phase = 0; phase < 2; ++phase) {
-            const bool use_a = (phase == 0) == a_fills;
-            const int* cand = use_a ? candA : candB;
-            const int nc = use_a ? na : nb;
-            for (int base = 0; base < nc; base += 32) {
-                const int j = base + lane;
-                unsigned st = 0;
-                int len = 0;
-                if (j < nc) {
-                    const int v = cand[j];
-                    if (!chosen_before(v, L1)) {
-                        st = g.rowptr[v];
-                        len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
-                        if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
-                    }
-                }
-                int pre;
-                const int M = warp_scan(len, pre);
-                for (int eb = 0; eb < M; eb += 32) {
-                    const int e = eb + lane;
-                    const int c = owner(pre, e);
-                    const unsigned stc = __shfl_sync(kFull, st, c);
-                    const int prc = __shfl_sync(kFull, pre, c);
-                    if (e < M) {
-                        const int x = g.col[stc + (e - prc)];
-                        if (!chosen_before(x, L1)) {
-                            if (phase == 0) {
-                                if (!pair_add(ptab, pmask, ep, x)) record_check(3, x, mins, pmask, 0, 0, 0);
-                            } else {
-                                sum += pair_get(ptab, pmask, ep, x);
-                            }
-                        }
-                    }
-                }
-                __syncwarp();
+        const int h = (don && split_min > 0 && ma + mb >= 64ll * split_min && nfill <= 0xffffff && nprobe <= 0xffffff)
+                          ? take_slot(L1)
+                          : -1;
+        if (h >= 0) {
+            const int fill_kind = kDonPairFill | (a_fills ? kDonSideA : 0);
+            const int probe_kind = kDonPairProbe | (a_fills ? 0 : kDonSideA);
+            unsigned gen = pair_publish(h, fill_kind, nfill, ep);
+            pair_slices(h, gen, fill_kind, fill, bnd, ptab, ep);
+            pair_wait(h, nfill);
+            gen = pair_publish(h, probe_kind, nprobe, ep);
+            sum += pair_slices(h, gen, probe_kind, probe, bnd, ptab, ep);
+            pair_wait(h, nprobe);
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();
+                atomicExch(&don->busy[h], 0u);
             }
+            __syncwarp();
+        } else {
+            pair_pass(fill, 0, nfill, bnd, ptab, ep, 0);
+            sum += pair_pass(probe, 0, nprobe, bnd, ptab, ep, 1);
         }
         sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
 #pragma unroll
@@ -960,7 +1096,7 @@ struct WarpCtx {
                 const unsigned gen = ((unsigned)(vr->word >> 48) + 1u) & 0xffffu;
                 vr->pair = pair_idx;
                 vr->depth = d;
-                vr->leaf = (d == P->L && batch_on()) ? 1 : 0;
+                vr->kind = (d == P->L && batch_on()) ? kDonLeaf : kDonLoop;
                 for (int j = 0; j < d; ++j) vr->chosen[j] = s->chosen[j];
                 __threadfence();
                 atomicExch(&r->word, don_pack(gen, (unsigned)e, 0u));
@@ -982,7 +1118,7 @@ struct WarpCtx {
             return false;
         }
         if (lane == 0) {
-            don_claim(&don->rec[s->dslot[d]], s->dgen[d], d == P->L && batch_on(), lo, hi);
+            don_claim(&don->rec[s->dslot[d]], s->dgen[d], (d == P->L && batch_on()) ? kDonLeaf : kDonLoop, lo, hi);
             if (hi > lo) {
                 s->idx[d] = lo;
                 s->end[d] = hi;
@@ -1108,7 +1244,8 @@ struct WarpCtx {
     // false when nothing could be taken.
     __device__ bool help_one(const PairDesc* pairs, int npairs, unsigned long long* out, int h, unsigned gen) {
         Donation* r = &don->rec[h];
-        int lo = 0, hi = 0, p = 0, d = 0, rend = 0;
+        int lo = 0, hi = 0, p = 0, d = 0, rend = 0, kind = 0, owner_w = 0;
+        unsigned ep = 0;
         if (lane == 0) {
             const unsigned long long w = *(volatile unsigned long long*)&r->word;
             if ((unsigned)(w >> 48) == gen && (w & 0xffffffu) < ((w >> 24) & 0xffffffu)) {
@@ -1117,10 +1254,12 @@ struct WarpCtx {
                 p = vr->pair;
                 d = vr->depth;
                 for (int j = 0; j < kMaxN; ++j) s->chosen[j] = j < d ? vr->chosen[j] : -1;
-                const bool leaf = vr->leaf != 0;
+                kind = vr->kind;
+                owner_w = vr->owner;
+                ep = vr->epoch;
                 rend = (int)((w >> 24) & 0xffffffu);
                 // the claim succeeds only while the record still holds these fields
-                don_claim(r, gen, leaf, lo, hi);
+                don_claim(r, gen, kind, lo, hi);
             }
         }
         lo = __shfl_sync(kFull, lo, 0);
@@ -1128,9 +1267,13 @@ struct WarpCtx {
         p = __shfl_sync(kFull, p, 0);
         d = __shfl_sync(kFull, d, 0);
         rend = __shfl_sync(kFull, rend, 0);
+        kind = __shfl_sync(kFull, kind, 0);
+        owner_w = __shfl_sync(kFull, owner_w, 0);
+        ep = __shfl_sync(kFull, ep, 0);
         __syncwarp();
         if (hi <= lo) return false;
-        if (p < 0 || p >= npairs) {
+        const bool pair_kind = (kind & 0xff) == kDonPairFill || (kind & 0xff) == kDonPairProbe;
+        if (p < 0 || p >= npairs || (pair_kind && (!ptab_base || (unsigned)owner_w >= gridDim.x * (blockDim.x >> 5)))) {
             if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
             __syncwarp();
             return true;
@@ -1140,21 +1283,46 @@ struct WarpCtx {
         g = pd.g;
         cap = pd.cap;
         pair_idx = p;
-        bool ok = d >= 2 && d <= P->L;
+        bool ok = d >= 2 && d <= P->L && (!pair_kind || (d == P->L - 1 && P->pair_ok));
         for (int l = 0; l < d && ok; ++l) {
             const int* nv;
             int dv;
             nbr(s->chosen[l], nv, dv);
             ok = build_chain(l, nv, dv);
         }
-        if (ok) {
-            start_level(d);
+        if (ok) start_level(d);
+        const int* cand = nullptr;
+        int bnd = 0;
+        if (ok && pair_kind) {
+            // the phase's side of the owner's pair sum, as the owner chose it
+            const int* candA;
+            const int* candB;
+            int na, nb;
+            pair_sides(candA, na, candB, nb, bnd);
+            const bool use_a = (kind & kDonSideA) != 0;
+            cand = use_a ? candA : candB;
+            ok = (use_a ? na : nb) == rend;
+        } else if (ok) {
             ok = s->end[d] == rend;
         }
         if (!ok) {
             // the rebuilt loop differs from the published one: the slice is lost
             if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
             __syncwarp();
+            return true;
+        }
+        if (pair_kind) {
+            unsigned long long* T = ptab_base + ((size_t)owner_w << pair_log2);
+            long long sum = pair_pass(cand, lo, hi, bnd, T, ep, (kind & 0xff) == kDonPairFill ? 0 : 1);
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence();
+                atomicAdd(&r->done, (unsigned)(hi - lo));
+            }
+            sum += pair_slices(h, gen, kind, cand, bnd, T, ep);
+#pragma unroll
+            for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+            if (lane == 0 && sum != 0) add128(out + 2 * p, (__int128)sum);
             return true;
         }
         __syncwarp();  // every lane has read end[d] above
@@ -1261,6 +1429,8 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match
     w.pair_on = pair_on && pair_tables != nullptr;
     w.pmask = (1u << pair_log2) - 1u;
     w.ptab = pair_tables ? pair_tables + ((size_t)gw << pair_log2) : nullptr;
+    w.ptab_base = pair_tables;
+    w.pair_log2 = pair_log2;
     if (lane == 0) w.s->epoch = 0;  // the first pair sum clears the table
     w.scratch = scratch_all + gw * scratch_per_warp;
     w.lane = lane;

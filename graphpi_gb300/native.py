@@ -48,6 +48,7 @@ SIGNATURES = {
     "gpm_graph_from_edges": (I32, [I32, C.c_int64, P, P, I32, C.POINTER(P)]),
     "gpm_graph_download": (I32, [P, P, P]),
     "gpm_graph_destroy": (I32, [P]),
+    "gpm_graph_device_csr": (I32, [P, I32, C.POINTER(P), C.POINTER(P)]),
     "gpm_graph_stats": (I32, [P, PI64, PI64, PI64, PI64]),
     "gpm_tri_count": (I32, [P, PU64]),
     "gpm_clique_count": (I32, [P, I32, C.POINTER(U128)]),

@@ -88,7 +88,17 @@ GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, c
  * neighbours; sizes from gpm_graph_stats) to host arrays. */
 GPM_API int gpm_graph_download(const gpm_graph* g, uint32_t* rowptr, int32_t* col);
 
-/* Frees a graph (the reference's ~Graph, include/graph.h:24-27). */
+/* Device pointers of the graph's resident CSR: the degree-relabelled copy
+ * the counting kernels use (caller_ids = 0) or the caller's numbering
+ * (caller_ids = 1; the same arrays when the graph was not relabelled).  They
+ * stay valid until gpm_graph_destroy.  For kernels built outside the engine
+ * (the per-schedule generated kernels) that count on the same numbering.
+ * No reference counterpart: the reference's Graph exposes its host arrays
+ * as public fields (include/graph.h:14-15). */
+GPM_API int gpm_graph_device_csr(const gpm_graph* g, int32_t caller_ids, const uint32_t** rowptr,
+                                 const int32_t** col);
+
+/* Frees a graph (the reference's ~Graph, include/graph.h:24-27). *//* Frees a graph (the reference's ~Graph, include/graph.h:24-27). */
 GPM_API int gpm_graph_destroy(gpm_graph* g);
 
 /* v_cnt, directed e_cnt, max degree and the largest possible intersection
