@@ -221,6 +221,8 @@ def run_ours(args, rank: int, world: int) -> dict | None:
             raise AssertionError("engine schedule tables differ from the reference's")
     red = [s.get_in_exclusion_optimize_redundancy() for s in scheds]
     n = len(scheds)
+    from graphpi_gb300 import autotune
+    tuned = autotune.apply_stored(g, scheds) if not args.no_tuning else None
     S = args.stripes or cfg["stripes"]
     timed_ids, warm_ids = step_ids(args, S)
     # rank r takes every world-th step of the sequence
@@ -409,6 +411,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "dtype": "int32 CSR / int128 counts",
         "data": "synthetic (seeded R-MAT generator)",
         "config": bench_config(args, cfg, S),
+        "tuning": ({k: v for k, v in tuned.items() if not k.startswith("_ms")} if tuned else "defaults"),
         "path": ("CUDA-graph replay of the batched launch (gpm_batch_exec_run)" if cfg["batched"]
                  else "one gpm_count launch per pattern"),
         "kernel_ms_per_step": statistics.median(kernel_ms),
@@ -544,6 +547,9 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
     ap.add_argument("--stripes", type=int, default=0, help="stripes per full job (0: the config's)")
+    ap.add_argument("--scale", type=int, default=0,
+                    help="R-MAT scale instead of the config's (small cases for profiling; no recorded sums)")
+    ap.add_argument("--no-tuning", action="store_true", help="ignore the stored autotuner table")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--generated", type=int, default=1, choices=[0, 1],
                     help="also time the per-schedule generated kernels on the same stripes")
@@ -560,6 +566,11 @@ def main() -> None:
         world = 1
     if args.warmup < 3:
         args.warmup = 3
+    if args.scale:
+        c = dict(CONFIGS[args.config])
+        c.update(scale=args.scale, golden=f"none_s{args.scale}",
+                 workload=c["workload"].replace(f"rmat_s{c['scale']}", f"rmat_s{args.scale}"))
+        CONFIGS[args.config] = c
     if args.impl == "reference":
         res = run_reference(args, rank, world)
     else:

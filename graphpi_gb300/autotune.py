@@ -15,6 +15,7 @@ Knobs (gpm_set_option):
   min_blocks                3: the kernel variant compiled for three 8-warp
                             blocks per SM (80 registers) instead of 122
   stage_max                 largest fixed set staged in shared memory (ints)
+  stage_tma                 stage those sets with bulk copies (cp.async.bulk)
   leaf_batch                batched deepest loop level on/off
   pair_leaf                 pair sums over the last two loops on/off
   bitmap_min                smallest fixed leaf set tested through a bitmap
@@ -42,6 +43,7 @@ SPACE = {
     "blocks_per_sm": [1, 2, 3],
     "min_blocks": [1, 3],
     "stage_max": [0, 256, 1024, 2048],
+    "stage_tma": [0, 1],
     "leaf_batch": [0, 1],
     "pair_leaf": [0, 1],
     "bitmap_min": [0, 1024, 4096, 16384],
@@ -113,13 +115,18 @@ class _Trial:
 
 
 def autotune(graph, schedules, stripes: int = 1024, sample_stripes: int = 2, repeats: int = 2,
-             budget_s: float = 90.0, space: dict | None = None, verbose: bool = False) -> dict:
-    """Returns the fastest knob table found (and leaves it applied)."""
+             budget_s: float = 90.0, space: dict | None = None, verbose: bool = False,
+             sample: list[int] | None = None) -> dict:
+    """Returns the fastest knob table found (and leaves it applied).  The
+    sample is `sample` (stripe ids of `stripes`), else sample_stripes evenly
+    spaced stripes."""
     from .api import Plan
     space = space or SPACE
     plans = [Plan(s) for s in schedules]
-    step = max(1, stripes // max(1, sample_stripes))
-    trial = _Trial(graph, plans, stripes, [i * step + step // 2 for i in range(sample_stripes)])
+    if sample is None:
+        step = max(1, stripes // max(1, sample_stripes))
+        sample = [i * step + step // 2 for i in range(sample_stripes)]
+    trial = _Trial(graph, plans, stripes, list(sample))
     t_start = time.time()
     best = current()
     apply(best)
@@ -201,18 +208,21 @@ def main(argv: list[str] | None = None) -> dict:
     ap = argparse.ArgumentParser()
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--seed", type=int, default=3)
-    ap.add_argument("--stripes", type=int, default=1 << 26, help="the sample is a few of this many stripes")
-    ap.add_argument("--samples", type=int, default=4)
+    ap.add_argument("--stripes", type=int, default=1 << 23, help="the sample is a few of this many stripes")
+    ap.add_argument("--samples", type=int, default=8)
+    ap.add_argument("--skip", type=int, default=48,
+                    help="the sample is drawn from the seeded random stripe ids after the first SKIP (the "
+                         "benchmark's timed and warm-up steps use the first ones)")
     ap.add_argument("--budget", type=float, default=120.0, help="seconds")
     ap.add_argument("--out", default=str(TUNED))
     a = ap.parse_args(argv)
     g = workloads.rmat_s22() if (a.scale, a.seed) == (22, 3) else workloads.rmat_scale(a.scale, a.seed)
     tri = g.triangle_counting_mt()
     scheds = [Schedule(p, 1, 1, True, g.v_cnt, g.e_cnt, tri) for p in motifs_3_to_5()]
-    table = autotune(g, scheds, stripes=a.stripes, sample_stripes=a.samples, repeats=1, budget_s=a.budget,
-                     verbose=True)
+    sample = workloads.random_stripes(a.stripes, a.skip + a.samples)[a.skip:]
+    table = autotune(g, scheds, stripes=a.stripes, sample=sample, repeats=1, budget_s=a.budget, verbose=True)
     table["_graph"] = f"rmat s{a.scale} seed {a.seed}"
-    table["_sample"] = f"{a.samples} of {a.stripes} stripes"
+    table["_sample"] = f"random stripes {sample} of {a.stripes}"
     Path(a.out).parent.mkdir(parents=True, exist_ok=True)
     save(table, a.out, signature(g, scheds))
     print(json.dumps(table, indent=1, sort_keys=True))

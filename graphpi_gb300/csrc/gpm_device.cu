@@ -43,6 +43,10 @@ namespace gpm {
 
 #include "match_core.cuh"
 
+// Bytes allocated past the end of every neighbour array and scratch area:
+// a bulk copy of a staged set covers the 16-byte aligned span around it.
+constexpr size_t kCsrSlack = 16;
+
 // Triangle count: sum over v, u in N(v) with u < v of |N(v) ∩ N(u) ∩ [0, u)|
 // (Graph::tc_mt / intersection_size_clique, src/graph.cpp:66-95,121-139).
 __global__ void __launch_bounds__(256) tc_kernel(GraphView g, unsigned long long* __restrict__ cursor,
@@ -364,7 +368,7 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     GPM_CK(cudaMalloc(&new_deg.p, sizeof(unsigned) * ((size_t)V + 1)));
     GPM_CK(cudaMalloc(&new_rowptr.p, sizeof(unsigned) * ((size_t)V + 1)));
     GPM_CK(cudaMalloc(&new_col_u.p, sizeof(int) * (size_t)E));
-    GPM_CK(cudaMalloc(&new_col.p, sizeof(int) * (size_t)E));
+    GPM_CK(cudaMalloc(&new_col.p, sizeof(int) * (size_t)E + kCsrSlack));
     relabel_maps_kernel<<<blocks, threads, 0, st>>>(g->rowptr, (const int*)order.p, V, (int*)new_id.p,
                                                     (unsigned*)new_deg.p);
     GPM_CK(cudaGetLastError());
@@ -494,7 +498,7 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
     }
     ls.wpb = (int)o.warps_per_block;
     ls.stage_cap = (int)o.stage_max;
-    ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)ls.stage_cap * ls.wpb;
+    ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)stage_stride(ls.stage_cap) * ls.wpb;
     ls.count_bytes = o.count_bytes != 0;
     ls.min_blocks = (o.min_blocks == 3 && !ls.count_bytes) ? 3 : 1;
     if (ls.min_blocks == 3 && ls.wpb > 8) {
@@ -535,7 +539,8 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         for (const PairDesc& d : ls.descs) fewest = std::min(fewest, (d.ntasks + stripes - 1) / stripes);
         ls.chunk = (int)std::max<unsigned long long>(1, std::min<unsigned long long>(o.chunk, fewest / warps));
     }
-    ls.leaf_on = (int)o.leaf_batch;
+    // bit 1: stage fixed sets with bulk copies (their sources carry the slack)
+    ls.leaf_on = (int)o.leaf_batch | (o.stage_tma ? 2 : 0);
     ls.pair_on = 0;
     if (o.pair_leaf) {
         bool any = false;
@@ -564,7 +569,7 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
     // two bitmaps over vertex ids per warp for the batched leaves
     ls.bm_words = 0;
     ls.bm_min = (int)o.bitmap_min;
-    if (ls.leaf_on && ls.bm_min > 0) {
+    if ((ls.leaf_on & 1) && ls.bm_min > 0) {
         int vmax = 0;
         bool any = false;
         for (int i = 0; i < n; ++i) {
@@ -613,7 +618,7 @@ static ScratchLayout scratch_layout(const LaunchSetup& ls) {
     b = (b + 255) & ~(size_t)255;
     s.dense = b;
     b += dense_bytes(ls);
-    s.total = std::max<size_t>(b, 1);
+    s.total = b + kCsrSlack;  // bulk copies of sets may round their end up by 12 bytes
     return s;
 }
 
@@ -788,7 +793,7 @@ GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_
     };
     cudaStream_t st = c->stream;
     if (cudaMalloc(&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
-        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(E, 1)) != cudaSuccess) {
+        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(E, 1) + kCsrSlack) != cudaSuccess) {
         set_error("gpm_graph_create: out of device memory for %llu edges", (unsigned long long)E);
         return fail(GPM_ERR_OOM);
     }
@@ -907,7 +912,7 @@ GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, c
     g->e_cnt = h_n;
     g->device = c->device;
     if (cudaMalloc(&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
-        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(h_n, 1)) != cudaSuccess) {
+        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(h_n, 1) + kCsrSlack) != cudaSuccess) {
         if (g->rowptr) cudaFree(g->rowptr);
         delete g;
         set_error("gpm_graph_from_edges: out of device memory for %llu edges", h_n);
@@ -1361,7 +1366,7 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     const Options& o = options();
     const int wpb = (int)o.warps_per_block;
     const int stage_cap = (int)o.stage_max;
-    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_cap * wpb;
+    const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_stride(stage_cap) * wpb;
     GPM_CK(cudaFuncSetAttribute(match_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     GPM_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, match_kernel<false, 1>, wpb * 32, smem));

@@ -21,6 +21,7 @@ struct Options {
     int64_t count_bytes = 0;    // 1: count algorithmic bytes
     int64_t timeout_ms = 2000;  // bounded device waits
     int64_t stage_max = 1024;   // largest fixed set staged in shared memory (ints)
+    int64_t stage_tma = 0;      // 1: stage fixed sets with bulk copies (cp.async.bulk) instead of loads
     int64_t leaf_batch = 0;     // 1: batched deepest level where the plan allows
     int64_t pair_leaf = 1;      // 1: pair sums over the last two levels where the plan allows
     int64_t dense_slots = 0;    // dense counter arrays for pair sums too big for a table (0 = none)

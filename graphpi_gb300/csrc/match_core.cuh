@@ -12,7 +12,12 @@ constexpr unsigned kFull = 0xffffffffu;
 // (a merge window that does not advance, an id outside the graph) writes a
 // code and a few values here and skips the work; the host reports it.
 // [0] code, [1..7] values.
-constexpr int kErrMergeStall = 1, kErrBadVertex = 2, kErrLoopIndex = 5, kErrSetSize = 6;
+constexpr int kErrMergeStall = 1, kErrBadVertex = 2, kErrLoopIndex = 5, kErrSetSize = 6, kErrStage = 7;
+
+// Ints per stage region of a warp: the staging capacity rounded up to 16
+// bytes plus 8 ints, so that a bulk copy of a 16-byte aligned span around a
+// set of stage_cap ints fits.
+__host__ __device__ constexpr int stage_stride(int stage_cap) { return ((stage_cap + 3) & ~3) + 8; }
 __device__ unsigned long long g_check[8];
 
 __device__ __noinline__ void record_check(int code, long long a, long long b, long long c, long long d, long long e,
@@ -47,7 +52,9 @@ struct PairDesc {
     int pad_;
 };
 
-struct WarpState {
+struct alignas(16) WarpState {
+    unsigned long long mbar;  // mbarrier of this warp's bulk copies into its stage
+    unsigned mphase;          // parity of the mbarrier's current phase
     int chosen[kMaxN];
     int idx[kMaxN];
     int end[kMaxN];
@@ -216,6 +223,32 @@ __device__ __forceinline__ bool prefer_merge(int na, int nb) {
     return (long long)na * lg * a4 >= 4ll * (long long)(na + nb);
 }
 
+// Warp galloping search: the position of the first element >= x in
+// B[lo, nb), for 32 keys at once (one per lane, ascending across lanes).
+// Lane i probes B[lo + 2^i - 1] — the whole exponential probe sequence in
+// one round of loads — then each lane finds its bracket among the probes
+// with a 5-step shuffle search and binary-searches inside it:
+// about log2(distance from lo) dependent loads instead of log2(nb - lo).
+// Every lane must call it (it shuffles).
+__device__ __forceinline__ int gallop_search(const int* B, int lo, int nb, int x, int lane) {
+    const long long off = (long long)lo + (1ll << lane) - 1;
+    const int pv = (lane < 31 && off < nb) ? B[off] : INT_MAX;
+    int pos = 0;  // probes below x
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        const int q = __shfl_sync(kFull, pv, pos + step - 1);
+        if (q < x) pos += step;
+    }
+    int l = pos == 0 ? lo : (int)min((long long)nb, (long long)lo + (1ll << (pos - 1)));
+    int h = pos >= 31 ? nb : (int)min((long long)nb, (long long)lo + (1ll << pos) - 1);
+    while (l < h) {
+        const int m = (l + h) >> 1;
+        if (B[m] < x) l = m + 1;
+        else h = m;
+    }
+    return l;
+}
+
 // A ∩ B written sorted to out; returns its size.
 __device__ int isect_store(const int* A, int na, const int* B, int nb, int* out, int lane) {
     if (na > nb) {
@@ -228,12 +261,7 @@ __device__ int isect_store(const int* A, int na, const int* B, int nb, int* out,
         const int i = base + lane;
         const bool valid = i < na;
         const int x = valid ? A[i] : INT_MAX;
-        int l = lo, h = nb;
-        while (l < h) {
-            int m = (l + h) >> 1;
-            if (B[m] < x) l = m + 1;
-            else h = m;
-        }
+        const int l = gallop_search(B, lo, nb, x, lane);
         const bool found = valid && l < nb && B[l] == x;
         const unsigned mask = __ballot_sync(kFull, found);
         if (found) out[written + __popc(mask & lanemask_lt())] = x;
@@ -259,12 +287,7 @@ __device__ int isect_count(const int* A, int na, const int* B, int nb, int bound
         const int i = base + lane;
         const bool valid = i < na;
         const int x = valid ? A[i] : INT_MAX;
-        int l = lo, h = nb;
-        while (l < h) {
-            int m = (l + h) >> 1;
-            if (B[m] < x) l = m + 1;
-            else h = m;
-        }
+        const int l = gallop_search(B, lo, nb, x, lane);
         bool found = valid && l < nb && B[l] == x;
         if (found)
             for (int j = 0; j < nch; ++j)
@@ -355,8 +378,9 @@ struct WarpCtx {
     int cap;
     int lane;
     int leaf_on;
-    int* stage;      // 2 * stage_cap ints of this warp's shared memory
+    int* stage;      // 2 * stage_stride(stage_cap) ints of this warp's shared memory
     int stage_cap;
+    int tma;         // 1: stage fixed sets with bulk copies
     int pair_on;
     unsigned long long* ptab;  // this warp's pair-sum table (pmask + 1 words)
     unsigned long long* ptab_base;  // every warp's tables, 2^pair_log2 words each
@@ -399,10 +423,51 @@ struct WarpCtx {
         return bm != nullptr && bm_min > 0 && n > stage_cap && n >= bm_min && tests >= 2ll * n;
     }
 
-    // copies a fixed set into shared-memory region r when it fits
+    // Copies a fixed set into shared-memory region r when it fits.  With
+    // tma on, one lane issues a 1-D bulk copy (cp.async.bulk, completion
+    // counted on the warp's mbarrier) of the 16-byte aligned span around the
+    // set — the set's start rounded down, its end rounded up — and every lane
+    // waits on the mbarrier; the set starts `off` ints into the region.  Set
+    // sources (the CSR and the per-warp scratch) carry 16 bytes of slack past
+    // their end for that round-up.
     __device__ const int* stage_set(const int* p, int n, int r) {
         if (n > stage_cap || n <= 0) return p;
-        int* dst = stage + r * stage_cap;
+        int* dst = stage + r * stage_stride(stage_cap);
+#ifndef GPM_EMU
+        if (tma) {
+            const unsigned long long src = (unsigned long long)p;
+            const unsigned long long a0 = src & ~15ull;
+            const unsigned bytes = (unsigned)(((src + 4ull * (unsigned long long)n - a0) + 15ull) & ~15ull);
+            const unsigned bar = (unsigned)__cvta_generic_to_shared(&s->mbar);
+            const unsigned sdst = (unsigned)__cvta_generic_to_shared(dst);
+            __syncwarp();  // every lane's earlier reads of the region come first
+            if (lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        sdst),
+                    "l"(a0), "r"(bytes), "r"(bar)
+                    : "memory");
+            }
+            const unsigned ph = s->mphase;
+            unsigned done = 0;
+            for (int it = 0; it < (1 << 22) && !done; ++it)
+                asm volatile(
+                    "{ .reg .pred q; mbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2; selp.u32 %0, 1, 0, q; }"
+                    : "=r"(done)
+                    : "r"(bar), "r"(ph)
+                    : "memory");
+            if (!__all_sync(kFull, done)) {
+                if (lane == 0) record_check(kErrStage, n, (long long)src, bytes, 0, 0, 0);
+            }
+            __syncwarp();
+            if (lane == 0) s->mphase = ph ^ 1u;
+            __syncwarp();
+            return dst + (int)((src - a0) >> 2);
+        }
+#endif
         for (int i = lane; i < n; i += 32) dst[i] = p[i];
         __syncwarp();
         return dst;
@@ -1423,9 +1488,23 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match
     const long long gw = (long long)blockIdx.x * nwarps + wid;
     WarpCtx<kBytes> w;
     w.s = reinterpret_cast<WarpState*>(smem_raw) + wid;
-    w.stage = reinterpret_cast<int*>(reinterpret_cast<WarpState*>(smem_raw) + nwarps) + (size_t)wid * 2 * stage_cap;
+    w.stage = reinterpret_cast<int*>(reinterpret_cast<WarpState*>(smem_raw) + nwarps) +
+              (size_t)wid * 2 * stage_stride(stage_cap);
     w.stage_cap = stage_cap;
-    w.leaf_on = leaf_on;
+    // leaf_on: bit 0 the batched deepest level, bit 1 bulk-copy staging
+    w.leaf_on = leaf_on & 1;
+    w.tma = (leaf_on >> 1) & 1;
+#ifndef GPM_EMU
+    if (w.tma) {
+        if (lane == 0) {
+            const unsigned bar = (unsigned)__cvta_generic_to_shared(&w.s->mbar);
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            w.s->mphase = 0;
+        }
+        __syncwarp();
+    }
+#endif
     w.pair_on = pair_on && pair_tables != nullptr;
     w.pmask = (1u << pair_log2) - 1u;
     w.ptab = pair_tables ? pair_tables + ((size_t)gw << pair_log2) : nullptr;

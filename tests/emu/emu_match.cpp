@@ -151,7 +151,7 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     std::vector<unsigned> bitmaps((size_t)warps * 2 * bm_words, 0u);
     DonationArea* don = k.split > 0 ? new DonationArea() : nullptr;
     if (don) std::memset((void*)don, 0, sizeof(DonationArea));
-    const size_t smem = sizeof(WarpState) * k.wpb + sizeof(int) * 2 * (size_t)k.stage_cap * k.wpb;
+    const size_t smem = sizeof(WarpState) * k.wpb + sizeof(int) * 2 * (size_t)stage_stride(k.stage_cap) * k.wpb;
     std::vector<std::vector<unsigned char>> shared(k.blocks, std::vector<unsigned char>(smem));
     gpm_emu::block_dim = {(unsigned)(k.wpb * 32), 1, 1};
     gpm_emu::grid_dim = {(unsigned)k.blocks, 1, 1};

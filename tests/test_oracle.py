@@ -179,3 +179,18 @@ def test_oracle_clique_path_counts_cliques(engine, oracle):
             assert oracle.count_clique(g, s) == want, k
             if k <= 5:
                 assert oracle.brute_force(g, gp.Pattern(k, True)) == want, k
+
+
+def test_unfolded_cpu_code_matches_oracle(engine, oracle):
+    """The unfolded CPU comparison path (oracle/unfolded.py: per-schedule
+    nested loops, as the reference's code generator writes them) counts what
+    the interpreted oracle counts, with and without inclusion-exclusion."""
+    from oracle.unfolded import Unfolded
+    g = gp.rmat(10, 12, 0.57, 0.19, 0.19, 6)
+    tri = oracle.triangles(g)
+    for iep in (True, False):
+        scheds = [gp.Schedule(p, 1, 1, iep, g.v_cnt, g.e_cnt, tri) for p in gp.motifs_3_to_5()]
+        scheds += [gp.Schedule(p, 1, 1, iep, g.v_cnt, g.e_cnt, tri) for p in gp.MotifGenerator(6).generate()[::23]]
+        u = Unfolded(scheds)
+        for i, s in enumerate(scheds):
+            assert u.count(g, i) == oracle.count(g, s), (i, iep)
