@@ -22,6 +22,7 @@ struct Options {
     int64_t timeout_ms = 2000;  // bounded device waits
     int64_t stage_max = 1024;   // largest fixed set staged in shared memory (ints)
     int64_t stage_tma = 0;      // 1: stage fixed sets with bulk copies (cp.async.bulk) instead of loads
+    int64_t schedule_gpu = 1;   // 1: Schedule scores its candidates on the GPU when one is present
     int64_t leaf_batch = 0;     // 1: batched deepest level where the plan allows
     int64_t pair_leaf = 1;      // 1: pair sums over the last two levels where the plan allows
     int64_t dense_slots = 0;    // dense counter arrays for pair sums too big for a table (0 = none)
@@ -88,6 +89,16 @@ struct DevPlan {
 };
 
 constexpr int kLeafGeneric = 0, kLeafCount = 1, kLeafIep2 = 2;
+
+// Scores schedule candidates on the GPU (schedule_gpu.cu): candidate c is
+// the pattern in loop order cand_order[c] (mats holds n*n ints per order)
+// with npairs[c] sorted restriction pairs (28 slots of two ints each in
+// pairs); perf is the performance model (1..3).  GPM_ERR_NO_DEVICE without a
+// GPU.  The values equal the host models' bit for bit.
+int score_candidates_gpu(int n, int perf, int pattern_max_degree, const std::vector<int>& mats,
+                         const std::vector<int>& cand_order, const std::vector<int>& npairs,
+                         const std::vector<int>& pairs, int v_cnt, unsigned int e_cnt, long long tri_cnt,
+                         std::vector<double>& vals);
 
 // Decodes gpm_schedule_build tables into a DevPlan (host).
 int compile_plan(const int64_t* t, int32_t n_words, DevPlan* out);

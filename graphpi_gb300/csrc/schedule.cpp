@@ -12,12 +12,14 @@
 // library is compiled with -ffp-contract=off so the choice does not change
 // between x86 and Arm hosts.
 #include "graphpi/schedule.h"
+#include "gpm_internal.h"
 
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
+#include <string>
 
 namespace {
 
@@ -227,34 +229,72 @@ Schedule::Schedule(const Pattern& pattern, bool& is_pattern_valid, int performan
             if (performance_modeling_type == 2) return GraphZero_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
             return Naive_estimate_schedule_restrict(order, pairs, v_cnt, e_cnt);
         };
-        // Every order is scored independently (in parallel); the choice is
-        // the reference's sequential one: the first strict minimum in order.
-        std::vector<double> order_val(candidates.size());
-        std::vector<PairList> order_pairs(candidates.size());
+        // The restriction options of every order (in parallel); an order
+        // with none is scored once without restrictions.
+        std::vector<std::vector<PairList> > opts(candidates.size());
 #pragma omp parallel for schedule(dynamic, 1)
         for (long i = 0; i < (long)candidates.size(); ++i) {
-            const std::vector<int>& order = candidates[i];
-            std::vector<int> cur = reorder(pattern.get_adj_mat_ptr(), n, order);
-            std::vector<PairList> options;
+            std::vector<int> cur = reorder(pattern.get_adj_mat_ptr(), n, candidates[i]);
             if (restricts_type == 1) {
-                restricts_generate(cur.data(), options);
+                restricts_generate(cur.data(), opts[i]);
             } else {
                 Schedule probe(cur.data(), n);
                 PairList pairs;
                 probe.GraphZero_aggressive_optimize(pairs);
-                options.push_back(pairs);
+                opts[i].push_back(pairs);
             }
+            if (opts[i].empty()) opts[i].push_back(PairList());
+        }
+        // Every candidate scored: on the GPU (one thread per candidate,
+        // explicitly rounded arithmetic in the host order, so the values are
+        // the host's bit for bit) when a device is present and the
+        // "schedule_gpu" option is on, else on the host cores.
+        std::vector<long> first(candidates.size() + 1, 0);
+        for (size_t i = 0; i < candidates.size(); ++i) first[i + 1] = first[i] + (long)opts[i].size();
+        std::vector<double> vals((size_t)first.back());
+        bool scored = false;
+#ifndef GPM_HOST_ONLY  // builds without the CUDA translation units score on the host
+        if (gpm::options().schedule_gpu) {
+            std::vector<int> mats, cand_order, npairs, flat;
+            for (size_t i = 0; i < candidates.size(); ++i) {
+                std::vector<int> cur = reorder(pattern.get_adj_mat_ptr(), n, candidates[i]);
+                mats.insert(mats.end(), cur.begin(), cur.end());
+                for (const auto& pairs : opts[i]) {
+                    PairList sorted = pairs;
+                    std::sort(sorted.begin(), sorted.end());
+                    cand_order.push_back((int)i);
+                    npairs.push_back((int)sorted.size());
+                    for (int q = 0; q < 28; ++q) {
+                        flat.push_back(q < (int)sorted.size() ? sorted[q].first : 0);
+                        flat.push_back(q < (int)sorted.size() ? sorted[q].second : 0);
+                    }
+                }
+            }
+            const bool fits = npairs.empty() || *std::max_element(npairs.begin(), npairs.end()) <= 28;
+            const int rc = fits ? gpm::score_candidates_gpu(n, performance_modeling_type, get_max_degree(), mats,
+                                                            cand_order, npairs, flat, v_cnt, e_cnt, tri_cnt, vals)
+                                : GPM_ERR_UNSUPPORTED;
+            if (rc == GPM_OK) scored = true;
+            else if (rc != GPM_ERR_NO_DEVICE && rc != GPM_ERR_UNSUPPORTED)
+                throw std::runtime_error(std::string("Schedule: ") + gpm_last_error());
+        }
+#endif
+        if (!scored) {
+#pragma omp parallel for schedule(dynamic, 1)
+            for (long i = 0; i < (long)candidates.size(); ++i)
+                for (size_t j = 0; j < opts[i].size(); ++j) vals[first[i] + j] = score(candidates[i], opts[i][j]);
+        }
+        // the reference's sequential choice: the first strict minimum in order
+        std::vector<double> order_val(candidates.size());
+        std::vector<PairList> order_pairs(candidates.size());
+        for (size_t i = 0; i < candidates.size(); ++i) {
             bool have = false;
-            if (options.empty()) {
-                order_val[i] = score(order, PairList());
-                have = true;
-            }
-            for (const auto& pairs : options) {
-                const double val = score(order, pairs);
+            for (size_t j = 0; j < opts[i].size(); ++j) {
+                const double val = vals[first[i] + j];
                 if (!have || val < order_val[i]) {
                     have = true;
                     order_val[i] = val;
-                    order_pairs[i] = pairs;
+                    order_pairs[i] = opts[i][j];
                 }
             }
         }

@@ -95,6 +95,29 @@ def _time_schedule(g: Graph, s: Schedule, max_launch_ms: float = 150.0, cap_ms: 
         plan.close()
 
 
+def _work_schedule(g: Graph, s: Schedule, stripes: int = 16) -> float:
+    """Algorithmic bytes of one stripe of the schedule's job, counted exactly
+    by the counting build of the kernel (the int32 elements the reference's
+    merges would read).  Loop sharing is off while counting, so the figure
+    does not depend on how warps happen to be scheduled: a deterministic
+    measure of a candidate's work."""
+    plan = Plan(s)
+    out = U128()
+    old = {k: native.get_option(k) for k in ("count_bytes", "split", "raw_sums", "stripes", "stripe")}
+    try:
+        native.set_option("count_bytes", 1)
+        native.set_option("split", 0)
+        native.set_option("raw_sums", 1)
+        native.set_option("stripes", stripes)
+        native.set_option("stripe", stripes // 2)
+        check(lib().gpm_count(g.device(), plan.handle, C.byref(out)), "gpm_count")
+        return float(native.last_launch_stats()[2])
+    finally:
+        for k, v in old.items():
+            native.set_option(k, v)
+        plan.close()
+
+
 def relativize(feats: np.ndarray) -> np.ndarray:
     """Features of one pattern's candidates relative to each other: the
     analytic cost terms become differences to the cheapest candidate, so the
@@ -106,8 +129,11 @@ def relativize(feats: np.ndarray) -> np.ndarray:
 
 
 def collect(g: Graph, patterns: list[Pattern], max_candidates: int = 32, use_iep: bool = True,
-            verbose: bool = False) -> list[dict]:
-    """Measures candidate schedules of every pattern on g (GPU)."""
+            verbose: bool = False, label: str = "ms") -> list[dict]:
+    """Measures candidate schedules of every pattern on g (GPU).  The label
+    each row is fitted to ("y") is the estimated kernel time in ms
+    (label="ms") or the exact algorithmic bytes of a fixed stripe of the job
+    (label="work", deterministic)."""
     stats = graph_stats(g)
     rows = []
     for pi, p in enumerate(patterns):
@@ -124,9 +150,10 @@ def collect(g: Graph, patterns: list[Pattern], max_candidates: int = 32, use_iep
         for i in idx:
             c = cands[i]
             s = schedule_from_order(p, c["order"], c["pairs"], use_iep, 1)
-            ms = _time_schedule(g, s)
+            y = _time_schedule(g, s) if label == "ms" else _work_schedule(g, s)
             mine.append({"pattern": pi, "cand": i, "features": schedule_features(s, stats, c["cost"]),
-                         "ms": ms, "cost": c["cost"], "order": c["order"], "pairs": c["pairs"]})
+                         "ms": y if label == "ms" else None, "y": y, "cost": c["cost"], "order": c["order"],
+                         "pairs": c["pairs"]})
         rel = relativize(np.stack([r["features"] for r in mine]))
         for r, f in zip(mine, rel):
             r["features"] = f
@@ -158,7 +185,7 @@ class CostModel:
         """Targets are log10 runtimes relative to the mean over the same
         pattern's candidates: only the order within a pattern matters."""
         X = np.stack([r["features"] for r in rows]).astype(np.float32)
-        logs = np.array([math.log10(max(r["ms"], 1e-3)) for r in rows], dtype=np.float64)
+        logs = np.array([math.log10(max(r["y"], 1e-3)) for r in rows], dtype=np.float64)
         pats = np.array([r["pattern"] for r in rows])
         y = np.zeros(len(rows), dtype=np.float32)
         for p in np.unique(pats):
@@ -242,13 +269,13 @@ def evaluate(rows: list[dict], model: CostModel, judge: int = 3, shortlist: int 
     for pi, rs in sorted(by_pat.items()):
         pred = model.predict(np.stack([r["features"] for r in rs]))
         order = np.argsort(pred)
-        m = rs[int(order[0])]["ms"]
+        m = rs[int(order[0])]["y"]
         by_cost = sorted(range(len(rs)), key=lambda i: (rs[i]["cost"], rs[i]["cand"]))
-        a = rs[by_cost[0]]["ms"]
+        a = rs[by_cost[0]]["y"]
         short = by_cost[:shortlist]
-        rr = rs[min(short, key=lambda i: (pred[i], i))]["ms"]
-        j = min([rs[int(i)]["ms"] for i in order[:judge]] + [a])
-        b = min(r["ms"] for r in rs)
+        rr = rs[min(short, key=lambda i: (pred[i], i))]["y"]
+        j = min([rs[int(i)]["y"] for i in order[:judge]] + [a])
+        b = min(r["y"] for r in rs)
         tot["mlp"] += m
         tot["rerank"] += rr
         tot["judged"] += j
@@ -280,19 +307,21 @@ def main(argv: list[str] | None = None) -> dict:
     ap.add_argument("--six-stride", type=int, default=8, help="every k-th of the 112 six-vertex motifs")
     ap.add_argument("--candidates", type=int, default=12)
     ap.add_argument("--epochs", type=int, default=3000)
+    ap.add_argument("--label", default="ms", choices=["ms", "work"],
+                    help="fit to measured kernel time or to exact algorithmic bytes of a fixed stripe")
     ap.add_argument("--out", default="")
     a = ap.parse_args(argv)
     t0 = time.time()
     pats = MotifGenerator(5).generate() + MotifGenerator(6).generate()[::a.six_stride]
     train, held = pats[::2], pats[1::2]
     g_tr = workloads.rmat_scale(a.train_scale, 2)
-    rows_tr = collect(g_tr, train, max_candidates=a.candidates)
+    rows_tr = collect(g_tr, train, max_candidates=a.candidates, label=a.label)
     g_ev = workloads.rmat_scale(a.eval_scale, 4)
-    rows_ev = collect(g_ev, held, max_candidates=a.candidates)
+    rows_ev = collect(g_ev, held, max_candidates=a.candidates, label=a.label)
     model = CostModel(hidden=64, seed=1)
     loss = model.fit(rows_tr, epochs=a.epochs)
     ev = evaluate(rows_ev, model)
-    res = {"train_graph": f"rmat s{a.train_scale}", "eval_graph": f"rmat s{a.eval_scale}",
+    res = {"label": a.label, "train_graph": f"rmat s{a.train_scale}", "eval_graph": f"rmat s{a.eval_scale}",
            "train_rows": len(rows_tr), "eval_rows": len(rows_ev), "train_loss": loss,
            "mlp_over_best": ev["mlp_over_best"], "rerank_over_best": ev["rerank_over_best"],
            "judged_over_best": ev["judged_over_best"], "analytic_over_best": ev["analytic_over_best"],

@@ -29,7 +29,8 @@ def _build() -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     jobs = [(["g++", "-std=c++20", *FLAGS, *INCLUDES, "-c", str(EMU / "emu_match.cpp"), "-o", str(OUT / "emu.o")])]
     for src in HOST_SOURCES:
-        jobs.append(["g++", "-std=c++17", *FLAGS, *INCLUDES, "-c", str(CSRC / src), "-o", str(OUT / (src + ".o"))])
+        jobs.append(["g++", "-std=c++17", *FLAGS, "-DGPM_HOST_ONLY", *INCLUDES, "-c", str(CSRC / src),
+                     "-o", str(OUT / (src + ".o"))])
     jobs.append(["gcc", *FLAGS, "-c", str(ROOT / "oracle" / "oracle.c"), "-o", str(OUT / "oracle.o")])
     procs = [subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True) for j in jobs]
     for j, p in zip(jobs, procs):
