@@ -527,6 +527,8 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         ls.blocks = (ls.blocks + 1) / 2;
     const int alpha4[3] = {(int)o.merge_alpha4[0], (int)o.merge_alpha4[1], (int)o.merge_alpha4[2]};
     GPM_CK(cudaMemcpyToSymbolAsync(c_merge_alpha4, alpha4, sizeof alpha4, 0, cudaMemcpyHostToDevice, c->stream));
+    const int mvec = (int)o.merge_vec;
+    GPM_CK(cudaMemcpyToSymbolAsync(c_merge_vec, &mvec, sizeof mvec, 0, cudaMemcpyHostToDevice, c->stream));
     const long long pair_max = (long long)o.pair_max_ops;
     GPM_CK(cudaMemcpyToSymbolAsync(c_pair_max_ops, &pair_max, sizeof pair_max, 0, cudaMemcpyHostToDevice, c->stream));
     // A grab takes `chunk` tasks of the stripe, but never leaves warps

@@ -34,6 +34,7 @@ struct Options {
     int64_t stripes = 1;        // a launch covers chunks q*stripes + stripe only
     int64_t stripe = 0;
     int64_t raw_sums = 0;       // 1: return undivided 128-bit sums
+    int64_t merge_vec = 0;      // 1: merges read 128-bit windows of the longer list
     int64_t merge_alpha4[3] = {4, 4, 4};  // merge-vs-search weight x4 per length bucket
 };
 Options& options();

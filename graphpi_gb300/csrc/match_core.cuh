@@ -206,6 +206,92 @@ __device__ int warp_merge(const int* A, int na, const int* B, int nb, int* out, 
     return acc;
 }
 
+// Merge variant with 128-bit window loads: each lane loads 4 consecutive
+// ints of B (one 16-byte load), so a step sees a 128-element window of B
+// against 32 elements of A.  The window starts at the 16-byte boundary at or
+// below B + j; its elements before j (already consumed, all below every
+// remaining A element) read as INT_MIN and are never counted, elements at or
+// past nb read as INT_MAX, and a lane whose 4 ints would cross nb loads them
+// one by one, so nothing past the list is read.  Each lane finds its A
+// element in the window: a 5-step shuffle search over the lanes' first
+// elements, then a look at that lane's 4 (and the next lane's first).  Used
+// when c_merge_vec is 1.
+template <bool kStore>
+__device__ int warp_merge4(const int* A, int na, const int* B, int nb, int* out, const int* chosen, int nch,
+                           int lane) {
+    int i = 0, j = 0, acc = 0;
+    while (i < na && j < nb) {
+        const int a = (i + lane < na) ? A[i + lane] : INT_MAX;
+        const int sh = (int)(((unsigned long long)(B + j) >> 2) & 3ull);
+        const int jb = j - sh;  // B + jb is 16-byte aligned
+        const int k0 = jb + 4 * lane;
+        int b[4];
+        if (k0 >= j && k0 + 3 < nb) {
+#ifdef GPM_EMU
+            for (int t = 0; t < 4; ++t) b[t] = B[k0 + t];
+#else
+            const int4 q = *reinterpret_cast<const int4*>(B + k0);
+            b[0] = q.x;
+            b[1] = q.y;
+            b[2] = q.z;
+            b[3] = q.w;
+#endif
+        } else {
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int k = k0 + t;
+                b[t] = k < j ? INT_MIN : (k < nb ? B[k] : INT_MAX);
+            }
+        }
+        // last lane whose first element is below a, then inside its four
+        int pos = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int f = __shfl_sync(kFull, b[0], pos + step);
+            if (pos + step < 32 && f < a) pos += step;
+        }
+        const int q0 = __shfl_sync(kFull, b[0], pos), q1 = __shfl_sync(kFull, b[1], pos),
+                  q2 = __shfl_sync(kFull, b[2], pos), q3 = __shfl_sync(kFull, b[3], pos);
+        const int nxt = __shfl_sync(kFull, b[0], (pos + 1) & 31);
+        bool found = (a != INT_MAX) &&
+                     (q0 == a || q1 == a || q2 == a || q3 == a || (pos < 31 && nxt == a));
+        if (!kStore && found)
+            for (int c = 0; c < nch; ++c)
+                if (chosen[c] == a) found = false;
+        const unsigned fm = __ballot_sync(kFull, found);
+        if (kStore && found) out[acc + __popc(fm & lanemask_lt())] = a;
+        acc += __popc(fm);
+        // consume A elements <= the window's last real element and B
+        // elements <= the A window's largest
+        int wlast = INT_MIN;
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (k0 + t >= j && k0 + t < nb) wlast = max(wlast, b[t]);
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) wlast = max(wlast, __shfl_xor_sync(kFull, wlast, o));
+        const int amax = __shfl_sync(kFull, a, 31);
+        int mine = 0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) mine += (k0 + t >= j && k0 + t < nb && b[t] <= amax) ? 1 : 0;
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) mine += __shfl_xor_sync(kFull, mine, o);
+        const int di = __popc(__ballot_sync(kFull, a <= wlast));
+        const int dj = mine;
+        if (di == 0 && dj == 0) {
+            const int a0 = __shfl_sync(kFull, a, 0);
+            if (lane == 0) record_check(kErrMergeStall, na, nb, i, j, a0, wlast);
+            break;
+        }
+        i += di;
+        j += dj;
+    }
+    if (kStore) __syncwarp();
+    return acc;
+}
+
+// 1: merges read B through 128-bit windows (warp_merge4); 0: one int per lane.
+__constant__ int c_merge_vec = 0;
+
 // Merge when both lists are of similar length: a binary-search round costs
 // about log2(nb) dependent loads for 32 elements of the short list, a merge
 // step one coalesced load per list for at least 32 elements.
@@ -255,7 +341,9 @@ __device__ int isect_store(const int* A, int na, const int* B, int nb, int* out,
         const int* t = A; A = B; B = t;
         int u = na; na = nb; nb = u;
     }
-    if (prefer_merge(na, nb)) return warp_merge<true>(A, na, B, nb, out, nullptr, 0, lane);
+    if (prefer_merge(na, nb))
+        return c_merge_vec ? warp_merge4<true>(A, na, B, nb, out, nullptr, 0, lane)
+                           : warp_merge<true>(A, na, B, nb, out, nullptr, 0, lane);
     int written = 0, lo = 0;
     for (int base = 0; base < na; base += 32) {
         const int i = base + lane;
@@ -281,7 +369,9 @@ __device__ int isect_count(const int* A, int na, const int* B, int nb, int bound
         const int* t = A; A = B; B = t;
         int u = na; na = nb; nb = u;
     }
-    if (prefer_merge(na, nb)) return warp_merge<false>(A, na, B, nb, nullptr, chosen, nch, lane);
+    if (prefer_merge(na, nb))
+        return c_merge_vec ? warp_merge4<false>(A, na, B, nb, nullptr, chosen, nch, lane)
+                           : warp_merge<false>(A, na, B, nb, nullptr, chosen, nch, lane);
     int cnt = 0, lo = 0;
     for (int base = 0; base < na; base += 32) {
         const int i = base + lane;

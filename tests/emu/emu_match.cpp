@@ -257,6 +257,23 @@ void case_donation() {
     expect_oracle("chung_lu_200 six-vertex", h, s6, k);
 }
 
+// the 128-bit window merge in every merge (alpha large: merges preferred)
+void case_vec() {
+    const Csr g = rmat(7, 10, 33);
+    std::vector<Sched> ss = motif_schedules(g, 5, true, 2);
+    for (const Sched& s : motif_schedules(g, 4, false, 1)) ss.push_back(s);
+    c_merge_vec = 1;
+    for (int a : {4, 1 << 20}) {
+        c_merge_alpha4[0] = c_merge_alpha4[1] = c_merge_alpha4[2] = a;
+        Knobs k;
+        k.split = 1;
+        k.leaf = 0;
+        expect_oracle("rmat8 vector merge", g, ss, k);
+    }
+    c_merge_alpha4[0] = c_merge_alpha4[1] = c_merge_alpha4[2] = 4;
+    c_merge_vec = 0;
+}
+
 // small enough for the CPU test suite: every path that donation touches
 void case_quick() {
     const Csr g = rmat(7, 8, 31);
@@ -353,13 +370,14 @@ void case_stripes() {
 int main(int argc, char** argv) {
     std::vector<std::string> cases;
     for (int i = 1; i < argc; ++i) cases.push_back(argv[i]);
-    if (cases.empty()) cases = {"quick", "pair", "stripes"};
+    if (cases.empty()) cases = {"quick", "pair", "stripes", "vec"};
     for (const std::string& c : cases) {
         if (c == "quick") case_quick();
         else if (c == "donation") case_donation();
         else if (c == "leafslices") case_leafslices();
         else if (c == "pair") case_pair();
         else if (c == "stripes") case_stripes();
+        else if (c == "vec") case_vec();
         else {
             std::fprintf(stderr, "unknown case %s\n", c.c_str());
             return 2;
