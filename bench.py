@@ -223,6 +223,11 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     n = len(scheds)
     from graphpi_gb300 import autotune
     tuned = autotune.apply_stored(g, scheds) if not args.no_tuning else None
+    forced = {}
+    for kv in args.set:
+        k, v = kv.split("=", 1)
+        gp.set_option(k, int(v))
+        forced[k] = int(v)
     S = args.stripes or cfg["stripes"]
     timed_ids, warm_ids = step_ids(args, S)
     # rank r takes every world-th step of the sequence
@@ -412,6 +417,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "data": "synthetic (seeded R-MAT generator)",
         "config": bench_config(args, cfg, S),
         "tuning": ({k: v for k, v in tuned.items() if not k.startswith("_ms")} if tuned else "defaults"),
+        "options_set": forced or None,
         "path": ("CUDA-graph replay of the batched launch (gpm_batch_exec_run)" if cfg["batched"]
                  else "one gpm_count launch per pattern"),
         "kernel_ms_per_step": statistics.median(kernel_ms),
@@ -550,6 +556,8 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=0,
                     help="R-MAT scale instead of the config's (small cases for profiling; no recorded sums)")
     ap.add_argument("--no-tuning", action="store_true", help="ignore the stored autotuner table")
+    ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE",
+                    help="engine option for this run (gpm_set_option), after the stored table")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--generated", type=int, default=1, choices=[0, 1],
                     help="also time the per-schedule generated kernels on the same stripes")

@@ -12,7 +12,8 @@ Knobs (gpm_set_option):
   chunk                     first-level tasks per work-queue grab
   warps_per_block           warps per persistent block
   blocks_per_sm             persistent blocks per SM
-  min_blocks                3: the kernel variant compiled for three 8-warp
+  merge_vec                 merges over 128-bit windows of the longer list
+  min_blocks                3 / 4: the kernel variants compiled for three / four 8-warp
                             blocks per SM (80 registers) instead of 122
   stage_max                 largest fixed set staged in shared memory (ints)
   stage_tma                 stage those sets with bulk copies (cp.async.bulk)
@@ -41,7 +42,8 @@ SPACE = {
     "chunk": [1, 2, 4, 8, 16, 32],
     "warps_per_block": [4, 8, 16],
     "blocks_per_sm": [1, 2, 3],
-    "min_blocks": [1, 3],
+    "min_blocks": [1, 3, 4],
+    "merge_vec": [0, 1],
     "stage_max": [0, 256, 1024, 2048],
     "stage_tma": [0, 1],
     "leaf_batch": [0, 1],

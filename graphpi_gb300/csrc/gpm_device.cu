@@ -181,12 +181,26 @@ __global__ void __launch_bounds__(256) clique_kernel(GraphView g, int k, unsigne
     if (lane == 0 && acc != 0) add128(out, acc);
 }
 
-// CSR checks: offsets monotone, ids in range, rows strictly increasing, no
-// self loops, every edge present in both directions.
-__global__ void validate_kernel(GraphView g, unsigned* __restrict__ flags) {
+// CSR checks in one streaming pass: offsets monotone, ids in range, rows
+// strictly increasing, no self loops, and symmetry.  Symmetry is checked
+// without searching: the sums over all directed edges (u, v) of two 64-bit
+// mixes of the key (u, v) must equal the sums over the reversed keys
+// (v, u); an edge list that is not symmetric passes only if two
+// independent 64-bit sums collide (about 2^-128 for any fixed input).
+// words[0]: flag bits (atomicOr on its low word), words[1..4]: the sums.
+__device__ __forceinline__ unsigned long long edge_mix(unsigned long long key, unsigned long long salt) {
+    unsigned long long z = key + salt;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+constexpr unsigned long long kSalt1 = 0x9E3779B97F4A7C15ull, kSalt2 = 0xD1B54A32D192ED03ull;
+
+__global__ void validate_kernel(GraphView g, unsigned long long* __restrict__ words) {
     const int lane = threadIdx.x & 31;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     unsigned bad = 0;
+    unsigned long long f1 = 0, b1 = 0, f2 = 0, b2 = 0;
     for (long long v = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < g.v_cnt; v += warps) {
         const unsigned a = g.rowptr[v], b = g.rowptr[v + 1];
         if (b < a || b > g.e_cnt) {
@@ -201,16 +215,35 @@ __global__ void validate_kernel(GraphView g, unsigned* __restrict__ flags) {
             }
             if (x == (int)v) bad |= 4;
             if (k > a && g.col[k - 1] >= x) bad |= 8;
-            const unsigned xa = g.rowptr[x], xb = g.rowptr[x + 1];
-            if (xb < xa || xb > g.e_cnt) {
-                bad |= 1;
-                continue;
-            }
-            const int p = lower_bound_u(g.col + xa, (int)(xb - xa), (int)v);
-            if (p >= (int)(xb - xa) || g.col[xa + p] != (int)v) bad |= 16;
+            const unsigned long long kf = ((unsigned long long)v << 32) | (unsigned)x;
+            const unsigned long long kb = ((unsigned long long)(unsigned)x << 32) | (unsigned long long)v;
+            f1 += edge_mix(kf, kSalt1);
+            b1 += edge_mix(kb, kSalt1);
+            f2 += edge_mix(kf, kSalt2);
+            b2 += edge_mix(kb, kSalt2);
         }
     }
-    if (bad) atomicOr(flags, bad);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        f1 += __shfl_xor_sync(kFull, f1, o);
+        b1 += __shfl_xor_sync(kFull, b1, o);
+        f2 += __shfl_xor_sync(kFull, f2, o);
+        b2 += __shfl_xor_sync(kFull, b2, o);
+    }
+    if (bad) atomicOr(reinterpret_cast<unsigned*>(words), bad);
+    if (lane == 0) {
+        atomicAdd(words + 1, f1);
+        atomicAdd(words + 2, b1);
+        atomicAdd(words + 3, f2);
+        atomicAdd(words + 4, b2);
+    }
+}
+
+// flag bits of a validate_kernel result (16: not symmetric)
+static unsigned csr_flags(const unsigned long long* w) {
+    unsigned f = (unsigned)(w[0] & 0xffffffffull);
+    if (w[1] != w[2] || w[3] != w[4]) f |= 16;
+    return f;
 }
 
 __global__ void degree_keys_kernel(const unsigned* __restrict__ rowptr, int v_cnt, unsigned* __restrict__ keys,
@@ -413,24 +446,25 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
 }
 
 static unsigned validate_csr(DeviceCtx* c, const GraphView& v, int* rc) {
-    unsigned* d_flags = nullptr;
-    unsigned flags = 0;
+    unsigned long long* d_words = nullptr;
+    unsigned long long w[5] = {0, 0, 0, 0, 0};
     *rc = GPM_OK;
-    if (cudaMalloc(&d_flags, sizeof(unsigned)) != cudaSuccess) {
+    if (cudaMalloc(&d_words, sizeof w) != cudaSuccess) {
         set_error("validate: out of device memory");
         *rc = GPM_ERR_OOM;
         return 0;
     }
-    cudaMemsetAsync(d_flags, 0, sizeof(unsigned), c->stream);
-    validate_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(v, d_flags);
-    cudaMemcpyAsync(&flags, d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+    cudaMemsetAsync(d_words, 0, sizeof w, c->stream);
+    validate_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(v, d_words);
+    cudaMemcpyAsync(w, d_words, sizeof w, cudaMemcpyDeviceToHost, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
-    cudaFree(d_flags);
+    cudaFree(d_words);
     if (e != cudaSuccess) {
         set_error("validate: %s", cudaGetErrorString(e));
         *rc = GPM_ERR_CUDA;
+        return 0;
     }
-    return flags;
+    return csr_flags(w);
 }
 
 static GraphView view_of(const gpm_graph* g, bool caller_ids = false) {
@@ -443,9 +477,9 @@ static GraphView view_of(const gpm_graph* g, bool caller_ids = false) {
     return v;
 }
 
-// Pair-sum tables: 2^pair_log2 64-bit words per warp, at most a quarter of
-// the free memory left after the set slots (2^13 .. 2^20 words unless forced).
-constexpr int kPairLog2Min = 13, kPairLog2Max = 20;
+// Pair-sum tables: 2^pair_log2 64-bit words per warp (2^17 unless forced or
+// a quarter of the free memory left after the set slots is less).
+constexpr int kPairLog2Min = 13, kPairLog2Default = 17;
 
 struct LaunchSetup {
     std::vector<PairDesc> descs;
@@ -461,7 +495,7 @@ struct LaunchSetup {
     int split_min = 0;
     int bm_words = 0;  // words per leaf bitmap (0: no bitmaps)
     int bm_min = 0;
-    int min_blocks = 1;  // kernel variant: 1 or 3 resident blocks per SM
+    int min_blocks = 1;  // kernel variant: 1, 3 or 4 resident blocks per SM
     int dense_slots = 0;  // pool of per-vertex counter arrays for big pair sums
     int dense_words = 0;
     bool count_bytes = false;
@@ -497,15 +531,18 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         nslots = std::max(nslots, p->host.nslots);
     }
     ls.wpb = (int)o.warps_per_block;
-    ls.stage_cap = (int)o.stage_max;
+    // the stage holds fixed sets of the batched leaf only: without it, no
+    // shared memory goes to staging (more blocks fit an SM)
+    ls.stage_cap = o.leaf_batch ? (int)o.stage_max : 0;
     ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)stage_stride(ls.stage_cap) * ls.wpb;
     ls.count_bytes = o.count_bytes != 0;
-    ls.min_blocks = (o.min_blocks == 3 && !ls.count_bytes) ? 3 : 1;
-    if (ls.min_blocks == 3 && ls.wpb > 8) {
-        set_error("min_blocks=3 needs warps_per_block <= 8 (got %d)", ls.wpb);
+    ls.min_blocks = ((o.min_blocks == 3 || o.min_blocks == 4) && !ls.count_bytes) ? (int)o.min_blocks : 1;
+    if (ls.min_blocks > 1 && ls.wpb > 8) {
+        set_error("min_blocks=%d needs warps_per_block <= 8 (got %d)", ls.min_blocks, ls.wpb);
         return GPM_ERR_INVALID_ARG;
     }
     const void* kfn = ls.count_bytes       ? (const void*)match_kernel<true, 1>
+                      : ls.min_blocks == 4 ? (const void*)match_kernel<false, 4>
                       : ls.min_blocks == 3 ? (const void*)match_kernel<false, 3>
                                            : (const void*)match_kernel<false, 1>;
     GPM_CK(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ls.smem));
@@ -556,7 +593,9 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
         if (o.pair_log2) {
             ls.pair_log2 = (int)o.pair_log2;
         } else {
-            ls.pair_log2 = kPairLog2Max;
+            // a fixed size (1 MB per warp), smaller only when memory is short:
+            // pair sums too big for it run on the shared dense arrays
+            ls.pair_log2 = kPairLog2Default;
             while (ls.pair_log2 > kPairLog2Min && warps * ((size_t)8 << ls.pair_log2) > room) --ls.pair_log2;
         }
         // dense counter arrays for the pair sums too big for a table: up to
@@ -654,6 +693,8 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
         ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, dense, ls.dense_slots, ls.dense_words, stats
     if (ls.count_bytes)
         match_kernel<true, 1><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
+    else if (ls.min_blocks == 4)
+        match_kernel<false, 4><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
     else if (ls.min_blocks == 3)
         match_kernel<false, 3><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
     else
@@ -727,17 +768,18 @@ static int finish_counts(int n, const gpm_plan* const* plans, const unsigned lon
 // Validates a freshly built device CSR and relabels it by degree.
 static int finish_graph(DeviceCtx* c, gpm_graph* g, bool relabel, const char* who) {
     cudaStream_t st = c->stream;
-    DevBuf d_flags;
-    GPM_CK(cudaMalloc(&d_flags.p, sizeof(unsigned)));
-    GPM_CK(cudaMemsetAsync(d_flags.p, 0, sizeof(unsigned), st));
-    validate_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), (unsigned*)d_flags.p);
-    unsigned flags = 0;
-    GPM_CK(cudaMemcpyAsync(&flags, d_flags.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    DevBuf d_words;
+    unsigned long long w[5] = {0, 0, 0, 0, 0};
+    GPM_CK(cudaMalloc(&d_words.p, sizeof w));
+    GPM_CK(cudaMemsetAsync(d_words.p, 0, sizeof w, st));
+    validate_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), (unsigned long long*)d_words.p);
+    GPM_CK(cudaMemcpyAsync(w, d_words.p, sizeof w, cudaMemcpyDeviceToHost, st));
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         set_error("%s: validation failed: %s", who, cudaGetErrorString(e));
         return GPM_ERR_CUDA;
     }
+    const unsigned flags = csr_flags(w);
     if (flags) {
         set_error("%s: malformed CSR (%s%s%s%s%s)", who, flags & 1 ? "offsets " : "",
                   flags & 2 ? "ids-out-of-range " : "", flags & 4 ? "self-loops " : "",
@@ -1329,7 +1371,7 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     }
     cudaStream_t st = cudaStreamPerThread;
     // control words: [0] work cursor, [1..2] 128-bit sum, [3..4] stats,
-    // [5..6] stripes/stripe, [7] max degree, [8] CSR check flags
+    // [5..6] stripes/stripe, [7] max degree, [8..12] CSR check words
     unsigned long long* ctrl = (unsigned long long*)base;
     PairDesc* d_pair = (PairDesc*)(base + 256);
     DevPlan* d_plan = (DevPlan*)(base + 512);
@@ -1347,16 +1389,16 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     view.v_cnt = v_cnt;
     view.pad_ = 0;
     view.e_cnt = e_cnt;
-    const unsigned long long init[9] = {0, 0, 0, 0, 0, 1, 0, 0, 0};
+    const unsigned long long init[13] = {0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0};
     GPM_CK(cudaMemcpyAsync(ctrl, init, sizeof init, cudaMemcpyHostToDevice, st));
     max_degree_kernel<<<sms * 4, 256, 0, st>>>(d_rowptr, v_cnt, (unsigned*)(ctrl + 7));
     GPM_CK(cudaGetLastError());
-    validate_kernel<<<sms * 8, 256, 0, st>>>(view, (unsigned*)(ctrl + 8));
+    validate_kernel<<<sms * 8, 256, 0, st>>>(view, ctrl + 8);
     GPM_CK(cudaGetLastError());
-    unsigned long long got[2] = {0, 0};
+    unsigned long long got[6] = {0, 0, 0, 0, 0, 0};
     GPM_CK(cudaMemcpyAsync(got, ctrl + 7, sizeof got, cudaMemcpyDeviceToHost, st));
     GPM_CK(cudaStreamSynchronize(st));
-    const unsigned maxdeg = (unsigned)got[0], flags = (unsigned)got[1];
+    const unsigned maxdeg = (unsigned)got[0], flags = csr_flags(got + 1);
     if (flags) {
         set_error("gpm_count_noalloc: malformed CSR (%s%s%s%s%s)", flags & 1 ? "offsets " : "",
                   flags & 2 ? "ids-out-of-range " : "", flags & 4 ? "self-loops " : "",
@@ -1367,7 +1409,7 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
     // (idle warps help with published loops until every warp is done)
     const Options& o = options();
     const int wpb = (int)o.warps_per_block;
-    const int stage_cap = (int)o.stage_max;
+    const int stage_cap = o.leaf_batch ? (int)o.stage_max : 0;
     const size_t smem = sizeof(WarpState) * wpb + sizeof(int) * 2 * (size_t)stage_stride(stage_cap) * wpb;
     GPM_CK(cudaFuncSetAttribute(match_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;

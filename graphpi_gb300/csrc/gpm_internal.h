@@ -25,9 +25,9 @@ struct Options {
     int64_t schedule_gpu = 1;   // 1: Schedule scores its candidates on the GPU when one is present
     int64_t leaf_batch = 0;     // 1: batched deepest level where the plan allows
     int64_t pair_leaf = 1;      // 1: pair sums over the last two levels where the plan allows
-    int64_t dense_slots = 0;    // dense counter arrays for pair sums too big for a table (0 = none)
+    int64_t dense_slots = 64;   // dense counter arrays for pair sums too big for a table (0 = none)
     int64_t pair_max_ops = 0;   // longest pair sum one warp takes on (0: no cap)
-    int64_t pair_log2 = 0;      // log2 entries of each warp's pair-sum table (0: sized to free memory)
+    int64_t pair_log2 = 0;      // log2 entries of each warp's pair-sum table (0: 17, less when memory is short)
     int64_t min_blocks = 1;     // 3: the kernel variant built for three 8-warp blocks per SM
     int64_t bitmap_min = 4096;  // fixed leaf sets this large are tested through a bitmap; 0 = never
     int64_t split = 64;         // loops this long (depth >= 2) are shared with idle warps; 0 = off

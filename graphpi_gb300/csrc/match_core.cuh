@@ -86,6 +86,16 @@ constexpr int kErrDonation = 4;
 // owner's table from the smaller side's candidates, then probing it with the
 // other side's (the owner waits until every slice of a phase is done).
 constexpr int kDonLoop = 0, kDonLeaf = 1, kDonPairFill = 2, kDonPairProbe = 3;
+// pair sums too big for a warp's table: a dense per-vertex counter array
+// from the pool, filled, probed and cleared again in three shared phases
+constexpr int kDonDenseFill = 4, kDonDenseProbe = 5, kDonDenseClear = 6;
+__device__ __forceinline__ bool don_pair_kind(int kind) { return (kind & 0xff) >= kDonPairFill && (kind & 0xff) <= kDonDenseClear; }
+__device__ __forceinline__ bool don_dense_kind(int kind) { return (kind & 0xff) >= kDonDenseFill && (kind & 0xff) <= kDonDenseClear; }
+// the pass a pair-sum phase runs: 0 insert / count, 1 probe / sum, 2 clear
+__device__ __forceinline__ int don_phase(int kind) {
+    const int k = kind & 0xff;
+    return (k == kDonPairFill || k == kDonDenseFill) ? 0 : ((k == kDonPairProbe || k == kDonDenseProbe) ? 1 : 2);
+}
 constexpr int kDonSideA = 0x100;  // pair-sum phases: the phase runs over side A (level L-1)
 
 struct Donation {
@@ -724,10 +734,12 @@ struct WarpCtx {
     }
 
     // One pass over the neighbour lists of cand[lo, hi) below bnd, for each
-    // element x not chosen before L-1: phase 0 adds one to x's count in table
-    // T (tag ep), phase 1 sums the counts (returns this lane's share).
-    __device__ long long pair_pass(const int* cand, int lo, int hi, int bnd, unsigned long long* T, unsigned ep,
-                                   int phase) {
+    // element x not chosen before L-1: phase 0 adds one to x's count, phase 1
+    // sums the counts (returns this lane's share), phase 2 zeroes them.  The
+    // counts live in the hash table T (tag ep) or, when cnt is set, in the
+    // dense counter array cnt indexed by vertex.
+    __device__ long long pair_pass(const int* cand, int lo, int hi, int bnd, unsigned long long* T, unsigned* cnt,
+                                   unsigned ep, int phase) {
         const int L1 = P->L - 1;
         long long sum = 0;
         for (int base = lo; base < hi; base += 32) {
@@ -752,7 +764,11 @@ struct WarpCtx {
                 if (e < M) {
                     const int x = g.col[stc + (e - prc)];
                     if (!chosen_before(x, L1)) {
-                        if (phase == 0) {
+                        if (cnt) {
+                            if (phase == 0) atomicAdd(&cnt[x], 1u);
+                            else if (phase == 1) sum += __ldcg(&cnt[x]);
+                            else cnt[x] = 0u;
+                        } else if (phase == 0) {
                             if (!pair_add(T, pmask, ep, x)) record_check(3, x, hi - lo, pmask, 0, 0, 0);
                         } else {
                             sum += pair_get(T, pmask, ep, x);
@@ -768,7 +784,7 @@ struct WarpCtx {
     // Publishes one phase of a shared pair sum in slot h (held by this warp):
     // n candidates, a new generation; returns the generation (lane 0's value
     // on every lane).
-    __device__ unsigned pair_publish(int h, int kind, int n, unsigned ep) {
+    __device__ unsigned pair_publish(int h, int kind, int n, unsigned ep, int owner_id) {
         unsigned gen = 0;
         __syncwarp();
         if (lane == 0) {
@@ -778,7 +794,7 @@ struct WarpCtx {
             vr->pair = pair_idx;
             vr->depth = P->L - 1;
             vr->kind = kind;
-            vr->owner = (int)gw;
+            vr->owner = owner_id;
             vr->epoch = ep;
             vr->done = 0u;
             for (int j = 0; j < P->L - 1; ++j) vr->chosen[j] = s->chosen[j];
@@ -792,7 +808,7 @@ struct WarpCtx {
     // cand until none is left; every finished slice is added to the
     // record's done count.  Returns this lane's share of the probe sums.
     __device__ long long pair_slices(int h, unsigned gen, int kind, const int* cand, int bnd,
-                                     unsigned long long* T, unsigned ep) {
+                                     unsigned long long* T, unsigned* cnt, unsigned ep) {
         Donation* r = &don->rec[h];
         long long sum = 0;
         for (;;) {
@@ -801,7 +817,7 @@ struct WarpCtx {
             lo = __shfl_sync(kFull, lo, 0);
             hi = __shfl_sync(kFull, hi, 0);
             if (hi <= lo) break;
-            sum += pair_pass(cand, lo, hi, bnd, T, ep, (kind & 0xff) == kDonPairFill ? 0 : 1);
+            sum += pair_pass(cand, lo, hi, bnd, T, cnt, ep, don_phase(kind));
             __syncwarp();
             if (lane == 0) {
                 __threadfence();  // the slice's table updates before its count
@@ -841,6 +857,61 @@ struct WarpCtx {
         return __shfl_sync(kFull, h, 0);
     }
 
+    // The pair sum with a dense counter array from the pool, shared with idle
+    // warps in three phases (count the fill side, sum over the probe side,
+    // zero the fill side's counters again), each finished by every helper
+    // before the next is published.  False (nothing done) when no array or
+    // no donation record is free.
+    __device__ bool pair_dense_shared(const int* candA, int na, const int* candB, int nb, int bnd, bool a_fills,
+                                      __int128& out) {
+        if (!dense || !don || split_min <= 0 || g.v_cnt > dense_words || na > 0xffffff || nb > 0xffffff) return false;
+        int slot = -1;
+        if (lane == 0) {
+            for (int i = 0; i < dense_slots && slot < 0; ++i) {
+                const int k = (int)((gw + i) % dense_slots);
+                if (atomicCAS(&dense_lock[k], 0u, 1u) == 0u) slot = k;
+            }
+        }
+        slot = __shfl_sync(kFull, slot, 0);
+        if (slot < 0) return false;
+        const int L1 = P->L - 1;
+        const int h = take_slot(L1 + 17);
+        if (h < 0) {
+            __syncwarp();
+            if (lane == 0) atomicExch(&dense_lock[slot], 0u);
+            __syncwarp();
+            return false;
+        }
+        unsigned* cnt = dense + (size_t)slot * (size_t)dense_words;
+        const int* fill = a_fills ? candA : candB;
+        const int nfill = a_fills ? na : nb;
+        const int* probe = a_fills ? candB : candA;
+        const int nprobe = a_fills ? nb : na;
+        const int fside = a_fills ? kDonSideA : 0, pside = a_fills ? 0 : kDonSideA;
+        long long sum = 0;
+        unsigned gen = pair_publish(h, kDonDenseFill | fside, nfill, 0u, slot);
+        pair_slices(h, gen, kDonDenseFill | fside, fill, bnd, nullptr, cnt, 0u);
+        pair_wait(h, nfill);
+        gen = pair_publish(h, kDonDenseProbe | pside, nprobe, 0u, slot);
+        sum += pair_slices(h, gen, kDonDenseProbe | pside, probe, bnd, nullptr, cnt, 0u);
+        pair_wait(h, nprobe);
+        gen = pair_publish(h, kDonDenseClear | fside, nfill, 0u, slot);
+        pair_slices(h, gen, kDonDenseClear | fside, fill, bnd, nullptr, cnt, 0u);
+        pair_wait(h, nfill);
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence();
+            atomicExch(&dense_lock[slot], 0u);
+            atomicExch(&don->busy[h], 0u);
+        }
+        __syncwarp();
+        sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
+        out = lane == 0 ? (__int128)sum : (__int128)0;
+        return true;
+    }
+
     // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
     // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
     // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
@@ -862,7 +933,12 @@ struct WarpCtx {
         if (c_pair_max_ops > 0 && ma + mb > c_pair_max_ops) return false;
         const long long mins = min(ma, mb);
         const bool a_fills = ma < mb;
-        if (mins * 2 > (long long)pmask + 1) return pair_level_dense(candA, na, candB, nb, bnd, a_fills, ma + mb + mins, out);
+        if (mins * 2 > (long long)pmask + 1) {
+            // too big for the table: a dense counter array, shared with idle
+            // warps when loops are shared, else one warp for bounded work
+            if (pair_dense_shared(candA, na, candB, nb, bnd, a_fills, out)) return true;
+            return pair_level_dense(candA, na, candB, nb, bnd, a_fills, ma + mb + mins, out);
+        }
         __syncwarp();
         if (lane == 0) {
             s->epoch = (s->epoch + 1) & 0xffffu;
@@ -885,11 +961,11 @@ struct WarpCtx {
         if (h >= 0) {
             const int fill_kind = kDonPairFill | (a_fills ? kDonSideA : 0);
             const int probe_kind = kDonPairProbe | (a_fills ? 0 : kDonSideA);
-            unsigned gen = pair_publish(h, fill_kind, nfill, ep);
-            pair_slices(h, gen, fill_kind, fill, bnd, ptab, ep);
+            unsigned gen = pair_publish(h, fill_kind, nfill, ep, (int)gw);
+            pair_slices(h, gen, fill_kind, fill, bnd, ptab, nullptr, ep);
             pair_wait(h, nfill);
-            gen = pair_publish(h, probe_kind, nprobe, ep);
-            sum += pair_slices(h, gen, probe_kind, probe, bnd, ptab, ep);
+            gen = pair_publish(h, probe_kind, nprobe, ep, (int)gw);
+            sum += pair_slices(h, gen, probe_kind, probe, bnd, ptab, nullptr, ep);
             pair_wait(h, nprobe);
             __syncwarp();
             if (lane == 0) {
@@ -898,8 +974,8 @@ struct WarpCtx {
             }
             __syncwarp();
         } else {
-            pair_pass(fill, 0, nfill, bnd, ptab, ep, 0);
-            sum += pair_pass(probe, 0, nprobe, bnd, ptab, ep, 1);
+            pair_pass(fill, 0, nfill, bnd, ptab, nullptr, ep, 0);
+            sum += pair_pass(probe, 0, nprobe, bnd, ptab, nullptr, ep, 1);
         }
         sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
 #pragma unroll
@@ -1427,8 +1503,11 @@ struct WarpCtx {
         ep = __shfl_sync(kFull, ep, 0);
         __syncwarp();
         if (hi <= lo) return false;
-        const bool pair_kind = (kind & 0xff) == kDonPairFill || (kind & 0xff) == kDonPairProbe;
-        if (p < 0 || p >= npairs || (pair_kind && (!ptab_base || (unsigned)owner_w >= gridDim.x * (blockDim.x >> 5)))) {
+        const bool pair_kind = don_pair_kind(kind);
+        const bool dense_kind = don_dense_kind(kind);
+        const bool bad_owner = pair_kind && (dense_kind ? (!dense || (unsigned)owner_w >= (unsigned)dense_slots)
+                                                       : (!ptab_base || (unsigned)owner_w >= gridDim.x * (blockDim.x >> 5)));
+        if (p < 0 || p >= npairs || bad_owner) {
             if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
             __syncwarp();
             return true;
@@ -1467,14 +1546,20 @@ struct WarpCtx {
             return true;
         }
         if (pair_kind) {
-            unsigned long long* T = ptab_base + ((size_t)owner_w << pair_log2);
-            long long sum = pair_pass(cand, lo, hi, bnd, T, ep, (kind & 0xff) == kDonPairFill ? 0 : 1);
+            unsigned long long* T = dense_kind ? nullptr : ptab_base + ((size_t)owner_w << pair_log2);
+            unsigned* cnt = dense_kind ? dense + (size_t)owner_w * (size_t)dense_words : nullptr;
+            if (dense_kind && g.v_cnt > dense_words) {
+                if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, -3);
+                __syncwarp();
+                return true;
+            }
+            long long sum = pair_pass(cand, lo, hi, bnd, T, cnt, ep, don_phase(kind));
             __syncwarp();
             if (lane == 0) {
                 __threadfence();
                 atomicAdd(&r->done, (unsigned)(hi - lo));
             }
-            sum += pair_slices(h, gen, kind, cand, bnd, T, ep);
+            sum += pair_slices(h, gen, kind, cand, bnd, T, cnt, ep);
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
             if (lane == 0 && sum != 0) add128(out + 2 * p, (__int128)sum);
@@ -1551,8 +1636,9 @@ struct WarpCtx {
     }
 };
 
-// kMinBlocks 1: any block up to 16 warps; 3: blocks of at most 8 warps, three
-// resident per SM (the register budget drops to 80, with a few spills)
+// kMinBlocks 1: any block up to 16 warps; 3 or 4: blocks of at most 8 warps,
+// three or four resident per SM (the register budget drops to 80 or 64, with
+// spills to local memory) for more warps in flight
 template <bool kBytes, int kMinBlocks>
 __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
                                                     unsigned long long* __restrict__ cursors,

@@ -296,18 +296,22 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
 
 /* Engine knobs (counts never depend on them):
  *   "warps_per_block", "blocks_per_sm", "chunk" (work-queue grab size),
- *   "min_blocks" (1, or 3: the kernel variant for three blocks of at most
- *   8 warps per SM),
+ *   "min_blocks" (1, or 3 / 4: the kernel variants for three / four blocks
+ *   of at most 8 warps per SM),
+ *   "stage_tma" (1: stage fixed leaf sets with bulk copies), "merge_vec"
+ *   (1: merges read 128-bit windows), "schedule_gpu" (1: Schedule scores
+ *   its candidates on the GPU when one is present),
  *   "split" (a loop at depth >= 2 with at least this many candidates is
  *   published so that idle warps take slices of it; 0 = off),
  *   "stage_max" (largest father set staged in shared memory),
  *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan
  *   allows; the pair-sum leaf is on by default, the batched leaf off),
  *   "pair_log2" (entries per warp of the pair-sum table as a power of two;
- *   0 = sized to free memory), "pair_max_ops" (longest pair sum one warp
+ *   0 = 2^17, fewer when memory is short), "pair_max_ops" (longest pair sum one warp
  *   takes on, in list elements; longer ones run as loops; 0 = no cap),
- *   "dense_slots" (per-vertex counter arrays shared by pair sums too big for
- *   the table; default 0 = none), "bitmap_min" (fixed leaf sets at least
+ *   "dense_slots" (per-vertex counter arrays for pair sums too big for the
+ *   table, filled and probed by idle warps together when "split" is on;
+ *   default 64), "bitmap_min" (fixed leaf sets at least
  *   this large are tested through a per-warp bitmap instead of a binary
  *   search; 0 = never),
  *   "merge_alpha4_small"/"_mid"/"_large" (merge vs search per length bucket),
