@@ -21,7 +21,7 @@ struct Options {
     int64_t count_bytes = 0;    // 1: count algorithmic bytes
     int64_t timeout_ms = 2000;  // bounded device waits
     int64_t stage_max = 1024;   // largest fixed set staged in shared memory (ints)
-    int64_t stage_tma = 0;      // 1: stage fixed sets with bulk copies (cp.async.bulk) instead of loads
+    int64_t stage_tma = 1;      // 1: stage fixed sets with bulk copies (cp.async.bulk) instead of loads
     int64_t schedule_gpu = 1;   // 1: Schedule scores its candidates on the GPU when one is present
     int64_t leaf_batch = 0;     // 1: batched deepest level where the plan allows
     int64_t pair_leaf = 1;      // 1: pair sums over the last two levels where the plan allows
@@ -34,7 +34,7 @@ struct Options {
     int64_t stripes = 1;        // a launch covers chunks q*stripes + stripe only
     int64_t stripe = 0;
     int64_t raw_sums = 0;       // 1: return undivided 128-bit sums
-    int64_t merge_vec = 0;      // 1: merges read 128-bit windows of the longer list
+    int64_t merge_vec = 1;      // 1: merges read 128-bit windows of the longer list
     int64_t merge_alpha4[3] = {4, 4, 4};  // merge-vs-search weight x4 per length bucket
 };
 Options& options();

@@ -300,7 +300,7 @@ __device__ int warp_merge4(const int* A, int na, const int* B, int nb, int* out,
 }
 
 // 1: merges read B through 128-bit windows (warp_merge4); 0: one int per lane.
-__constant__ int c_merge_vec = 0;
+__constant__ int c_merge_vec = 1;
 
 // Merge when both lists are of similar length: a binary-search round costs
 // about log2(nb) dependent loads for 32 elements of the short list, a merge

@@ -262,6 +262,7 @@ void case_vec() {
     const Csr g = rmat(7, 10, 33);
     std::vector<Sched> ss = motif_schedules(g, 5, true, 2);
     for (const Sched& s : motif_schedules(g, 4, false, 1)) ss.push_back(s);
+    const int saved = c_merge_vec;
     c_merge_vec = 1;
     for (int a : {4, 1 << 20}) {
         c_merge_alpha4[0] = c_merge_alpha4[1] = c_merge_alpha4[2] = a;
@@ -271,7 +272,14 @@ void case_vec() {
         expect_oracle("rmat8 vector merge", g, ss, k);
     }
     c_merge_alpha4[0] = c_merge_alpha4[1] = c_merge_alpha4[2] = 4;
-    c_merge_vec = 0;
+    c_merge_vec = 0;  // and the 32-wide merge on the same plans
+    {
+        Knobs k;
+        k.split = 1;
+        k.leaf = 0;
+        expect_oracle("rmat7 scalar merge", g, ss, k);
+    }
+    c_merge_vec = saved;
 }
 
 // small enough for the CPU test suite: every path that donation touches
