@@ -679,11 +679,11 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "pair_max_ops") slot = &o.pair_max_ops, lo = 0, hi = (int64_t)1 << 40;
     else if (k == "bitmap_min") slot = &o.bitmap_min, lo = 0, hi = 1 << 30;
     else if (k == "min_blocks") {
-        if (value != 1 && value != 3 && value != 4) {
-            set_error("gpm_set_option: min_blocks is 1, 3 or 4");
+        if (value != 1 && value != 3 && value != 4 && value != 5) {
+            set_error("gpm_set_option: min_blocks is 1, 3, 4 or 5");
             return GPM_ERR_INVALID_ARG;
         }
-        slot = &o.min_blocks, lo = 1, hi = 4;
+        slot = &o.min_blocks, lo = 1, hi = 5;
     }
     else if (k == "split") slot = &o.split, lo = 0, hi = 1 << 30;
     else if (k == "stripes") slot = &o.stripes, lo = 1, hi = 1 << 30;

@@ -536,12 +536,14 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
     ls.stage_cap = o.leaf_batch ? (int)o.stage_max : 0;
     ls.smem = sizeof(WarpState) * ls.wpb + sizeof(int) * 2 * (size_t)stage_stride(ls.stage_cap) * ls.wpb;
     ls.count_bytes = o.count_bytes != 0;
-    ls.min_blocks = ((o.min_blocks == 3 || o.min_blocks == 4) && !ls.count_bytes) ? (int)o.min_blocks : 1;
-    if (ls.min_blocks > 1 && ls.wpb > 8) {
-        set_error("min_blocks=%d needs warps_per_block <= 8 (got %d)", ls.min_blocks, ls.wpb);
+    ls.min_blocks = ((o.min_blocks >= 3 && o.min_blocks <= 5) && !ls.count_bytes) ? (int)o.min_blocks : 1;
+    if (ls.min_blocks > 1 && ls.wpb > (ls.min_blocks == 5 ? 4 : 8)) {
+        set_error("min_blocks=%d needs warps_per_block <= %d (got %d)", ls.min_blocks, ls.min_blocks == 5 ? 4 : 8,
+                  ls.wpb);
         return GPM_ERR_INVALID_ARG;
     }
     const void* kfn = ls.count_bytes       ? (const void*)match_kernel<true, 1>
+                      : ls.min_blocks == 5 ? (const void*)match_kernel<false, 5>
                       : ls.min_blocks == 4 ? (const void*)match_kernel<false, 4>
                       : ls.min_blocks == 3 ? (const void*)match_kernel<false, 3>
                                            : (const void*)match_kernel<false, 1>;
@@ -693,6 +695,8 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
         ls.pair_log2, don, ls.split_min, bitmaps, ls.bm_words, ls.bm_min, dense, ls.dense_slots, ls.dense_words, stats
     if (ls.count_bytes)
         match_kernel<true, 1><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
+    else if (ls.min_blocks == 5)
+        match_kernel<false, 5><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
     else if (ls.min_blocks == 4)
         match_kernel<false, 4><<<(unsigned)ls.blocks, ls.wpb * 32, ls.smem, st>>>(GPM_MATCH_ARGS);
     else if (ls.min_blocks == 3)

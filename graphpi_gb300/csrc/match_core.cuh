@@ -1638,9 +1638,10 @@ struct WarpCtx {
 
 // kMinBlocks 1: any block up to 16 warps; 3 or 4: blocks of at most 8 warps,
 // three or four resident per SM (the register budget drops to 80 or 64, with
-// spills to local memory) for more warps in flight
+// spills to local memory); 5: blocks of at most 4 warps, five per SM (96
+// registers, few spills) — more warps in flight
 template <bool kBytes, int kMinBlocks>
-__global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : 256, kMinBlocks) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
+__global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : (kMinBlocks == 5 ? 128 : 256), kMinBlocks) match_kernel(const PairDesc* __restrict__ pairs, int npairs,
                                                     unsigned long long* __restrict__ cursors,
                                                     unsigned long long* __restrict__ out, int* __restrict__ scratch_all,
                                                     long long scratch_per_warp, int chunk,
