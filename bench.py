@@ -202,6 +202,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
+    free0 = torch.cuda.mem_get_info(dev)[0]
     t = time.time()
     g = workloads.rmat_scale(cfg["scale"], cfg["seed"])
     gen_s = time.time() - t
@@ -272,6 +273,9 @@ def run_ours(args, rank: int, world: int) -> dict | None:
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    # device memory the engine holds for this workload (graph copies, plans,
+    # launch scratch), from the free memory before and after the warm-up
+    engine_bytes = free0 - torch.cuda.mem_get_info(dev)[0]
     kernel_ms, emb, raws_all = [], 0.0, []
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev) as clocks:
@@ -437,6 +441,7 @@ def run_ours(args, rank: int, world: int) -> dict | None:
         "clocks": clocks.summary(),
         "cpu_baseline": cpu,
         "setup_s": {"generate": round(gen_s, 2), "upload_relabel": round(upload_s, 3)},
+        "device_memory_gb": round(engine_bytes / 1e9, 2),
     }
     if gen_ms:
         res["generated"] = {

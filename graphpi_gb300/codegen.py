@@ -39,7 +39,6 @@ from pathlib import Path
 import numpy as np
 
 from . import native
-from .native import U128
 
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
