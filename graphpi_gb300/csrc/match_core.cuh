@@ -114,7 +114,8 @@ struct DonationArea {
     Donation rec[kDonSlots];
     unsigned busy[kDonSlots];  // 1 while a record's owner holds the slot
     unsigned finished;         // warps done with their own queues
-    unsigned pad_[3];
+    unsigned held;             // slots held by owners (records that may be live)
+    unsigned pad_[2];
 };
 
 __device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned end, unsigned next) {
@@ -853,6 +854,7 @@ struct WarpCtx {
                 const int c = (int)((gw * 7 + salt * 131 + probe * 257) & (kDonSlots - 1));
                 if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
             }
+            if (h >= 0) atomicAdd(&don->held, 1u);
         }
         return __shfl_sync(kFull, h, 0);
     }
@@ -903,6 +905,7 @@ struct WarpCtx {
             __threadfence();
             atomicExch(&dense_lock[slot], 0u);
             atomicExch(&don->busy[h], 0u);
+            atomicAdd(&don->held, ~0u);  // minus one
         }
         __syncwarp();
         sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
@@ -971,6 +974,7 @@ struct WarpCtx {
             if (lane == 0) {
                 __threadfence();
                 atomicExch(&don->busy[h], 0u);
+                atomicAdd(&don->held, ~0u);  // minus one
             }
             __syncwarp();
         } else {
@@ -1322,6 +1326,7 @@ struct WarpCtx {
                 if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
             }
             if (h >= 0) {
+                atomicAdd(&don->held, 1u);
                 Donation* r = &don->rec[h];
                 volatile Donation* vr = r;
                 const unsigned gen = ((unsigned)(vr->word >> 48) + 1u) & 0xffffu;
@@ -1368,6 +1373,7 @@ struct WarpCtx {
             if (s->downer[d] && (unsigned)s->dslot[d] < (unsigned)kDonSlots) {
                 __threadfence();
                 atomicExch(&don->busy[s->dslot[d]], 0u);
+                atomicAdd(&don->held, ~0u);  // minus one
             }
             s->dslot[d] = -1;
         }
@@ -1582,11 +1588,16 @@ struct WarpCtx {
     // After the warp's own queues: helps published loops until every warp
     // is done.  The host clamps the grid to the blocks that are resident at
     // once, so every other warp is running and the wait ends when they do;
-    // the polling is bounded all the same (2^22 rounds of at least 16 us).
+    // the polling is bounded all the same (2^24 rounds of at least 4 us; a
+    // helper that stops early only leaves work to the owners).  The records
+    // are scanned only while some owner holds a slot.
     __device__ void help_all(const PairDesc* pairs, int npairs, unsigned long long* out, unsigned total_warps) {
-        for (unsigned round = 0; round < (1u << 22); ++round) {
+        for (unsigned round = 0; round < (1u << 24); ++round) {
             bool worked = false;
-            for (int base = 0; base < kDonSlots; base += 32) {
+            unsigned held = 0;
+            if (lane == 0) held = *(volatile unsigned*)&don->held;
+            held = __shfl_sync(kFull, held, 0);
+            for (int base = 0; held && base < kDonSlots; base += 32) {
                 const int h = (int)((gw * 37 + base + lane) & (kDonSlots - 1));
                 const unsigned long long w = *(volatile unsigned long long*)&don->rec[h].word;
                 const bool live = (w & 0xffffffu) < ((w >> 24) & 0xffffffu);
@@ -1604,7 +1615,7 @@ struct WarpCtx {
             unsigned fin = 0;
             if (lane == 0) fin = *(volatile unsigned*)&don->finished;
             if (__shfl_sync(kFull, fin, 0) >= total_warps) return;
-            __nanosleep(16000);
+            __nanosleep(held ? 8000 : 4000);
         }
     }
 
