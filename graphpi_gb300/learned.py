@@ -164,7 +164,14 @@ def collect(g: Graph, patterns: list[Pattern], max_candidates: int = 32, use_iep
 
 
 class CostModel:
-    """MLP over standardised features predicting log10(ms)."""
+    """MLP over standardised features that corrects the analytic model.
+
+    Targets are a candidate's measured log10 runtime (or work) relative to the
+    other candidates of its pattern; the analytic model's relative log cost
+    (feature 26 after `relativize`) is the prior, and the network learns the
+    residual.  A prediction is prior + network output, so an untrained or
+    strongly regularised network ranks candidates as the analytic model does,
+    and what the network adds is the learned correction."""
 
     def __init__(self, hidden: int = 64, seed: int = 1):
         self.hidden = hidden
@@ -191,6 +198,10 @@ class CostModel:
         for p in np.unique(pats):
             m = pats == p
             y[m] = (logs[m] - logs[m].mean()).astype(np.float32)
+        prior = X[:, 26].astype(np.float64)
+        for p in np.unique(pats):
+            m = pats == p
+            y[m] -= (prior[m] - prior[m].mean()).astype(np.float32)
         self.mu = X.mean(axis=0)
         self.sd = X.std(axis=0) + 1e-3
         Xs = self._x(X)
@@ -200,6 +211,13 @@ class CostModel:
         return loss.value
 
     def predict(self, feats: np.ndarray) -> np.ndarray:
+        """Relative log10 runtime (work) of candidates: the analytic prior
+        plus the network's correction."""
+        f = np.atleast_2d(feats)
+        return f[:, 26].astype(np.float32) + self.correction(f)
+
+    def correction(self, feats: np.ndarray) -> np.ndarray:
+        """The network's output alone (the learned correction to the prior)."""
         Xs = self._x(np.atleast_2d(feats))
         y = np.zeros(len(Xs), dtype=np.float32)
         check(lib().gpm_mlp_forward(self.h, Xs.ctypes.data, len(Xs), y.ctypes.data), "gpm_mlp_forward")
