@@ -557,7 +557,8 @@ static int prepare_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gp
     }
     // the 3-block variant launches three blocks per SM when they fit
     ls.blocks = (long long)c->num_sms * std::min<long long>(std::max<long long>(o.blocks_per_sm, ls.min_blocks), occ);
-    ls.per_warp = (long long)nslots * cap;
+    // set slots, then the pair sums' two block-sum arrays at the end
+    ls.per_warp = (long long)nslots * cap + 2 * pair_bs_stride(cap);
     // shrink the grid when the per-warp scratch would not fit in free memory
     size_t free_b = 0, total_b = 0;
     GPM_CK(cudaMemGetInfo(&free_b, &total_b));
@@ -1423,13 +1424,13 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
         return GPM_ERR_INVALID_ARG;
     }
     const long long cap = std::max<long long>(1, maxdeg);
-    const long long per_warp = (long long)hp.nslots * cap;
+    const long long per_warp = (long long)hp.nslots * cap + 2 * pair_bs_stride(cap);
     const long long fit = (long long)(scratch_room / ((size_t)per_warp * sizeof(int)));
     const long long want = (long long)sms * std::min<long long>(o.blocks_per_sm, occ) * wpb;
     const long long warps = std::min(want, fit) / wpb * wpb;
     if (warps < wpb) {
         set_error("gpm_count_noalloc: one block of %d warps needs %lld bytes of scratch (%d sets x largest degree %lld "
-                  "x 4 bytes per warp); the allocation-free scratch holds %zu bytes: use gpm_count",
+                  "x 4 bytes per warp, and a tail of 1/16 of a set); the allocation-free scratch holds %zu bytes: use gpm_count",
                   wpb, (long long)wpb * per_warp * 4, hp.nslots, cap, scratch_room);
         return GPM_ERR_UNSUPPORTED;
     }

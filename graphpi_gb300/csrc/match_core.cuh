@@ -89,24 +89,44 @@ constexpr int kDonLoop = 0, kDonLeaf = 1, kDonPairFill = 2, kDonPairProbe = 3;
 // pair sums too big for a warp's table: a dense per-vertex counter array
 // from the pool, filled, probed and cleared again in three shared phases
 constexpr int kDonDenseFill = 4, kDonDenseProbe = 5, kDonDenseClear = 6;
-__device__ __forceinline__ bool don_pair_kind(int kind) { return (kind & 0xff) >= kDonPairFill && (kind & 0xff) <= kDonDenseClear; }
+// the first phase of a long pair sum: the candidates' list lengths below the
+// bound, in blocks of 32 candidates (the element phases are sliced by them)
+constexpr int kDonPairLen = 7;
+__device__ __forceinline__ bool don_pair_kind(int kind) { return (kind & 0xff) >= kDonPairFill && (kind & 0xff) <= kDonPairLen; }
 __device__ __forceinline__ bool don_dense_kind(int kind) { return (kind & 0xff) >= kDonDenseFill && (kind & 0xff) <= kDonDenseClear; }
-// the pass a pair-sum phase runs: 0 insert / count, 1 probe / sum, 2 clear
+// the pass a pair-sum element phase runs: 0 insert / count, 1 probe / sum, 2 clear
 __device__ __forceinline__ int don_phase(int kind) {
     const int k = kind & 0xff;
     return (k == kDonPairFill || k == kDonDenseFill) ? 0 : ((k == kDonPairProbe || k == kDonDenseProbe) ? 1 : 2);
 }
-constexpr int kDonSideA = 0x100;  // pair-sum phases: the phase runs over side A (level L-1)
+// pair-sum element phases: the phase runs over side A (level L-1); bits 16+
+// hold log2 of the elements per unit
+constexpr int kDonSideA = 0x100;
+
+// Pair sums share their length phase from this many blocks of 32 candidates
+// on, and slice their element phases in units of 2^GPM_PAIR_UNIT_LOG2
+// elements (the emulated-warp tests build with 1 and 0: every phase shared,
+// one-element units).
+#ifndef GPM_PAIR_SHARE_BLOCKS
+#define GPM_PAIR_SHARE_BLOCKS 8
+#endif
+#ifndef GPM_PAIR_UNIT_LOG2
+#define GPM_PAIR_UNIT_LOG2 6
+#endif
+
+// Words of each warp's scratch tail that hold a pair sum's block sums per
+// side (one word per 32 candidates of a list of at most cap).
+__host__ __device__ constexpr long long pair_bs_stride(long long cap) { return ((cap + 31) / 32 + 4) & ~3ll; }
 
 struct Donation {
     unsigned long long word;  // generation (16 bits) | end (24) | next (24)
     int pair;
     int depth;
-    int chosen[kMaxN];
+    int chosen[kMaxN];  // pair sums: chosen[0, L-1), and in the last word the phase side's candidate count
     int kind;        // kDon*
-    int owner;       // pair sums: global warp index of the table's owner
-    unsigned epoch;  // pair sums: tag of the owner's live table entries
-    unsigned done;   // pair sums: candidates of the phase finished
+    int owner;       // pair sums: global warp index of the owner (its arrays and table)
+    unsigned epoch;  // pair sums: tag of the owner's live table entries, or the dense array's index
+    unsigned done;   // pair sums: units of the phase finished
 };
 static_assert(sizeof(Donation) == 64, "one record per 64 bytes");
 
@@ -130,11 +150,13 @@ __device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned en
 __device__ void don_claim(Donation* r, unsigned gen, int kind, int& lo, int& hi) {
     lo = hi = 0;
     unsigned long long w = *(volatile unsigned long long*)&r->word;
-    // slice bounds per kind: loops [1, 64], batched leaves [8, 128], pair-sum
-    // phases [1, 16] candidates (each carries a whole neighbour list)
+    // slice bounds per kind: a loop's first slice for a helper one candidate
+    // (its later slices are weighted by claim_more), batched leaves [8, 128],
+    // pair-sum lengths [1, 16] blocks of 32 candidates, pair-sum element
+    // phases [1, 64] units (of 64 elements or more)
     kind &= 0xff;
     const unsigned smin = kind == kDonLeaf ? 8u : 1u;
-    const unsigned smax = kind == kDonLeaf ? 128u : (kind == kDonLoop ? 64u : 16u);
+    const unsigned smax = kind == kDonLeaf ? 128u : (kind == kDonLoop ? 1u : (kind == kDonPairLen ? 16u : 64u));
     for (int tries = 0; tries < (1 << 25); ++tries) {
         if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
         const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
@@ -498,6 +520,7 @@ struct WarpCtx {
     int bm_min;                // smallest fixed set tested through a bitmap
     int pair_idx;              // pair whose work is running
     long long gw;              // global warp index
+    long long spw;             // ints of scratch per warp (warp w's region: scratch + (w - gw) * spw)
     unsigned long long bytes;
 
     // Bitmap variant of a membership test: marks set S[0, n) in bitmap r.
@@ -604,103 +627,6 @@ struct WarpCtx {
         return hit;
     }
 
-    // c term of a pair sum: v in both candidate lists pairs with itself,
-    // contributing |N(v) ∩ [0, bnd) \ chosen| (this lane's share)
-    __device__ long long pair_c_term(const int* candA, int na, const int* candB, int nb, int bnd, int L1) {
-        long long sum = 0;
-        for (int base = 0; base < na; base += 32) {
-            const int j = base + lane;
-            if (j < na) {
-                const int v = candA[j];
-                if (!chosen_before(v, L1) && contains(candB, nb, v)) {
-                    const unsigned st = g.rowptr[v];
-                    const int* nv = g.col + st;
-                    const int len = lower_bound_u(nv, (int)(g.rowptr[v + 1] - st), bnd);
-                    int in = 0;
-                    for (int q = 0; q < L1; ++q) in += contains(nv, len, s->chosen[q]) ? 1 : 0;
-                    sum += (long long)(len - in);
-                }
-            }
-        }
-        return sum;
-    }
-
-    // Neighbour lists of cand[0, n) below bnd, for each element x not chosen
-    // before depth L1: op 0 adds one to cnt[x], op 1 sums cnt[x], op 2 zeroes it.
-    __device__ long long dense_pass(const int* cand, int n, int bnd, int L1, unsigned* cnt, int op) {
-        long long sum = 0;
-        for (int base = 0; base < n; base += 32) {
-            const int j = base + lane;
-            unsigned st = 0;
-            int len = 0;
-            if (j < n) {
-                const int v = cand[j];
-                if (!chosen_before(v, L1)) {
-                    st = g.rowptr[v];
-                    len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
-                    if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
-                }
-            }
-            int pre;
-            const int M = warp_scan(len, pre);
-            for (int eb = 0; eb < M; eb += 32) {
-                const int e = eb + lane;
-                const int c = owner(pre, e);
-                const unsigned stc = __shfl_sync(kFull, st, c);
-                const int prc = __shfl_sync(kFull, pre, c);
-                if (e < M) {
-                    const int x = g.col[stc + (e - prc)];
-                    if (!chosen_before(x, L1)) {
-                        if (op == 0) atomicAdd(&cnt[x], 1u);
-                        else if (op == 1) sum += __ldcg(&cnt[x]);
-                        else cnt[x] = 0u;
-                    }
-                }
-            }
-        }
-        return sum;
-    }
-
-    // The pair sum of pair_level with a dense counter array from the pool
-    // when its hash table is too small: O(mA + 2 mB) direct-indexed updates
-    // instead of |A| loops over B's lists.  Returns false (nothing done) when
-    // the work would be too long for one warp or no array is free; the lock
-    // is a try-lock, so no warp waits.
-    __device__ bool pair_level_dense(const int* candA, int na, const int* candB, int nb, int bnd, bool a_fills,
-                                     long long ops, __int128& out) {
-        constexpr long long kDenseMaxOps = 1ll << 24;
-        if (!dense || ops > kDenseMaxOps || g.v_cnt > dense_words) return false;
-        int slot = -1;
-        if (lane == 0) {
-            for (int i = 0; i < dense_slots && slot < 0; ++i) {
-                const int k = (int)((gw + i) % dense_slots);
-                if (atomicCAS(&dense_lock[k], 0u, 1u) == 0u) slot = k;
-            }
-        }
-        slot = __shfl_sync(kFull, slot, 0);
-        if (slot < 0) return false;
-        unsigned* cnt = dense + (size_t)slot * (size_t)dense_words;
-        const int L1 = P->L - 1;
-        const int* fill = a_fills ? candA : candB;
-        const int nfill = a_fills ? na : nb;
-        const int* probe = a_fills ? candB : candA;
-        const int nprobe = a_fills ? nb : na;
-        dense_pass(fill, nfill, bnd, L1, cnt, 0);
-        __threadfence();
-        __syncwarp();
-        long long sum = dense_pass(probe, nprobe, bnd, L1, cnt, 1);
-        __syncwarp();
-        dense_pass(fill, nfill, bnd, L1, cnt, 2);
-        __threadfence();
-        __syncwarp();
-        if (lane == 0) atomicExch(&dense_lock[slot], 0u);
-        sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-        out = lane == 0 ? (__int128)sum : (__int128)0;
-        return true;
-    }
-
     // The two sides of the pair sum of level L-1 (whose loop list is set):
     // the level L-1 candidates A, the level L candidates B (below their
     // bound; neither depends on v_{L-1}) and the tail's bound.
@@ -714,65 +640,158 @@ struct WarpCtx {
         bnd = bound_of(P->T);
     }
 
-    // Σ over the candidates not chosen before L-1 of |N(w) ∩ [0, bnd)| (warp-uniform)
-    __device__ long long side_total(const int* cand, int nc, int bnd) {
-        const int L1 = P->L - 1;
-        long long m = 0;
-        for (int base = 0; base < nc; base += 32) {
-            const int j = base + lane;
-            int len = 0;
-            if (j < nc) {
-                const int w = cand[j];
-                if (!chosen_before(w, L1)) {
-                    const unsigned st = g.rowptr[w];
-                    len = lower_bound_u(g.col + st, (int)(g.rowptr[w + 1] - st), bnd);
-                }
-            }
-            int pre;
-            m += warp_scan(len, pre);
-        }
-        return m;
+    // Pair sums run over the two candidate lists of pair_sides, A (level
+    // L-1) and B (level L), with every candidate's list length below the
+    // tail bound (0 for a candidate chosen before L-1): len[j] for each
+    // candidate and, per block of 32 candidates, the inclusive prefix sum of
+    // the block totals.  Those arrays live in the owner's scratch: the
+    // lengths in its two temporary slots (unused by pair plans, which have
+    // no inclusion–exclusion tail), the block sums at the end of its region.
+    // A phase then covers a flat range of list elements, so a slice is a
+    // bounded number of elements wherever the hubs among the candidates sit.
+    struct PairCtx {
+        const int* candA;
+        const int* candB;
+        int na, nb, bnd;
+        unsigned* lenA;
+        unsigned* lenB;
+        unsigned* bsA;
+        unsigned* bsB;
+        unsigned long long* T;  // table phases: the owner's hash table
+        unsigned* cnt;          // dense phases: the owner's counter array
+        unsigned ep;            // the table's tag
+    };
+
+    __device__ void pair_ctx(PairCtx& c, long long owner_w) {
+        pair_sides(c.candA, c.na, c.candB, c.nb, c.bnd);
+        int* base = scratch + (owner_w - gw) * spw;
+        c.lenA = reinterpret_cast<unsigned*>(base + (size_t)(P->nslots - 2) * cap);
+        c.lenB = reinterpret_cast<unsigned*>(base + (size_t)(P->nslots - 1) * cap);
+        const long long S = pair_bs_stride(cap);
+        c.bsA = reinterpret_cast<unsigned*>(base + spw - 2 * S);
+        c.bsB = reinterpret_cast<unsigned*>(base + spw - S);
+        c.T = nullptr;
+        c.cnt = nullptr;
+        c.ep = 0;
     }
 
-    // One pass over the neighbour lists of cand[lo, hi) below bnd, for each
-    // element x not chosen before L-1: phase 0 adds one to x's count, phase 1
-    // sums the counts (returns this lane's share), phase 2 zeroes them.  The
-    // counts live in the hash table T (tag ep) or, when cnt is set, in the
-    // dense counter array cnt indexed by vertex.
-    __device__ long long pair_pass(const int* cand, int lo, int hi, int bnd, unsigned long long* T, unsigned* cnt,
-                                   unsigned ep, int phase) {
+    // Length units [lo, hi): blocks of 32 candidates, side A's blocks first.
+    // Writes each candidate's length and each block's total.
+    __device__ void pair_length_blocks(const PairCtx& c, int lo, int hi) {
         const int L1 = P->L - 1;
-        long long sum = 0;
-        for (int base = lo; base < hi; base += 32) {
-            const int j = base + lane;
-            unsigned st = 0;
-            int len = 0;
-            if (j < hi) {
+        const int nba = (c.na + 31) >> 5;
+        for (int u = lo; u < hi; ++u) {
+            const bool sa = u < nba;
+            const int b = sa ? u : u - nba;
+            const int* cand = sa ? c.candA : c.candB;
+            const int n = sa ? c.na : c.nb;
+            unsigned* len = sa ? c.lenA : c.lenB;
+            unsigned* bs = sa ? c.bsA : c.bsB;
+            const int j = (b << 5) + lane;
+            int l = 0;
+            if (j < n) {
                 const int v = cand[j];
                 if (!chosen_before(v, L1)) {
-                    st = g.rowptr[v];
-                    len = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), bnd);
-                    if (kBytes) bytes += 4ull * (unsigned long long)len + 8;
+                    const unsigned st = g.rowptr[v];
+                    l = lower_bound_u(g.col + st, (int)(g.rowptr[v + 1] - st), c.bnd);
                 }
+                len[j] = (unsigned)l;
             }
             int pre;
-            const int M = warp_scan(len, pre);
+            const int tot = warp_scan(l, pre);
+            if (lane == 0) bs[b] = (unsigned)tot;
+        }
+        __syncwarp();
+    }
+
+    // bs[0, nblk) <- inclusive prefix sums in place; returns the total (the
+    // candidates are distinct vertices, so it is below the edge count < 2^32)
+    __device__ unsigned pair_scan(unsigned* bs, int nblk) {
+        unsigned carry = 0;
+        for (int base = 0; base < nblk; base += 32) {
+            const int b = base + lane;
+            unsigned incl = b < nblk ? __ldcg(&bs[b]) : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (b < nblk) bs[b] = carry + incl;
+            carry += __shfl_sync(kFull, incl, 31);
+        }
+        __syncwarp();
+        return carry;
+    }
+
+    // The block holding element e0: the number of blocks whose inclusive sum
+    // is at most e0 (a 32-way search: each step probes 32 evenly spaced
+    // blocks and keeps the gap where the sums pass e0).
+    __device__ int pair_first_block(const unsigned* bs, int nblk, unsigned long long e0) const {
+        int lo = 0, hi = nblk;  // the answer is in [lo, hi]
+        while (hi - lo > 32) {
+            const int step = (hi - lo + 31) >> 5;
+            const int p = lo + (lane + 1) * step - 1;
+            const bool le = p < hi && (unsigned long long)__ldcg(&bs[p]) <= e0;
+            const int c = __popc(__ballot_sync(kFull, le));
+            const int pc = lo + (c + 1) * step - 1;  // first probe above e0, if any
+            if (pc < hi) hi = pc;
+            lo += c * step;
+        }
+        const bool le = lo + lane < hi && (unsigned long long)__ldcg(&bs[lo + lane]) <= e0;
+        return lo + __popc(__ballot_sync(kFull, le));
+    }
+
+    // Elements [e0, e1) of one side's concatenated neighbour lists (below
+    // the bound), each x not chosen before L-1: phase 0 adds one to x's
+    // count, phase 1 sums the counts (this lane's share), phase 2 zeroes
+    // them.  Counts live in the table T (tag ep) or, when cnt is set, in the
+    // dense array cnt indexed by vertex.  In phase 1 a candidate w that is on
+    // the other side too (`other`) pairs with itself once per element:
+    // those are the v == w terms of sum_x a_x b_x, subtracted here.
+    __device__ long long pair_flat(const int* cand, int n, const unsigned* len, const unsigned* bs, const int* other,
+                                   int nother, unsigned long long* T, unsigned* cnt, unsigned ep, int phase,
+                                   unsigned long long e0, unsigned long long e1) {
+        const int L1 = P->L - 1;
+        const int nblk = (n + 31) >> 5;
+        long long sum = 0;
+        for (int b = pair_first_block(bs, nblk, e0); b < nblk; ++b) {
+            const unsigned long long b0 = b ? (unsigned long long)__ldcg(&bs[b - 1]) : 0ull;
+            if (b0 >= e1) break;
+            const int j = (b << 5) + lane;
+            const int l = j < n ? (int)__ldcg(&len[j]) : 0;
+            int pre;
+            warp_scan(l, pre);
+            const unsigned long long s0 = b0 + (unsigned)pre, s1 = s0 + (unsigned)l;
+            const unsigned long long a = s0 > e0 ? s0 : e0, z = s1 < e1 ? s1 : e1;
+            int m = 0;
+            unsigned st = 0;
+            int dup = 0;
+            if (a < z) {
+                m = (int)(z - a);
+                const int v = cand[j];
+                st = g.rowptr[v] + (unsigned)(a - s0);
+                if (phase == 1) dup = contains(other, nother, v) ? 1 : 0;
+                if (kBytes) bytes += 4ull * (unsigned long long)m + 8;
+            }
+            int pm;
+            const int M = warp_scan(m, pm);
             for (int eb = 0; eb < M; eb += 32) {
                 const int e = eb + lane;
-                const int c = owner(pre, e);
+                const int c = owner(pm, e);
                 const unsigned stc = __shfl_sync(kFull, st, c);
-                const int prc = __shfl_sync(kFull, pre, c);
+                const int pc = __shfl_sync(kFull, pm, c);
+                const int dc = __shfl_sync(kFull, dup, c);
                 if (e < M) {
-                    const int x = g.col[stc + (e - prc)];
+                    const int x = g.col[stc + (e - pc)];
                     if (!chosen_before(x, L1)) {
                         if (cnt) {
                             if (phase == 0) atomicAdd(&cnt[x], 1u);
-                            else if (phase == 1) sum += __ldcg(&cnt[x]);
+                            else if (phase == 1) sum += (long long)__ldcg(&cnt[x]) - dc;
                             else cnt[x] = 0u;
                         } else if (phase == 0) {
-                            if (!pair_add(T, pmask, ep, x)) record_check(3, x, hi - lo, pmask, 0, 0, 0);
+                            if (!pair_add(T, pmask, ep, x)) record_check(3, x, n, pmask, 0, 0, 0);
                         } else {
-                            sum += pair_get(T, pmask, ep, x);
+                            sum += (long long)pair_get(T, pmask, ep, x) - dc;
                         }
                     }
                 }
@@ -782,10 +801,25 @@ struct WarpCtx {
         return sum;
     }
 
-    // Publishes one phase of a shared pair sum in slot h (held by this warp):
-    // n candidates, a new generation; returns the generation (lane 0's value
-    // on every lane).
-    __device__ unsigned pair_publish(int h, int kind, int n, unsigned ep, int owner_id) {
+    // One slice [lo, hi) of a pair-sum phase; returns this lane's share of
+    // the probe sums.  Element phases count units of 2^(kind >> 16) elements.
+    __device__ long long pair_run(const PairCtx& c, int kind, int lo, int hi) {
+        if ((kind & 0xff) == kDonPairLen) {
+            pair_length_blocks(c, lo, hi);
+            return 0;
+        }
+        const bool sa = (kind & kDonSideA) != 0;
+        const int ul = (kind >> 16) & 31;
+        return pair_flat(sa ? c.candA : c.candB, sa ? c.na : c.nb, sa ? c.lenA : c.lenB, sa ? c.bsA : c.bsB,
+                         sa ? c.candB : c.candA, sa ? c.nb : c.na, c.T, c.cnt, c.ep, don_phase(kind),
+                         (unsigned long long)lo << ul, (unsigned long long)hi << ul);
+    }
+
+    // Publishes one phase of a shared pair sum in slot h (held by this
+    // warp): `units` units, a new generation; tag is the table's epoch or
+    // the dense array's index, aux the side's candidate count (the length
+    // phase: side A's).  Returns the generation (on every lane).
+    __device__ unsigned pair_publish(int h, int kind, int units, unsigned tag, int aux) {
         unsigned gen = 0;
         __syncwarp();
         if (lane == 0) {
@@ -795,21 +829,21 @@ struct WarpCtx {
             vr->pair = pair_idx;
             vr->depth = P->L - 1;
             vr->kind = kind;
-            vr->owner = owner_id;
-            vr->epoch = ep;
+            vr->owner = (int)gw;
+            vr->epoch = tag;
             vr->done = 0u;
             for (int j = 0; j < P->L - 1; ++j) vr->chosen[j] = s->chosen[j];
+            vr->chosen[kMaxN - 1] = aux;
             __threadfence();
-            atomicExch(&r->word, don_pack(gen, (unsigned)n, 0u));
+            atomicExch(&r->word, don_pack(gen, (unsigned)units, 0u));
         }
         return __shfl_sync(kFull, gen, 0);
     }
 
-    // Takes slices of one pair-sum phase (record h, generation gen) over
-    // cand until none is left; every finished slice is added to the
-    // record's done count.  Returns this lane's share of the probe sums.
-    __device__ long long pair_slices(int h, unsigned gen, int kind, const int* cand, int bnd,
-                                     unsigned long long* T, unsigned* cnt, unsigned ep) {
+    // Takes slices of one pair-sum phase (record h, generation gen) until
+    // none is left; every finished slice is added to the record's done
+    // count.  Returns this lane's share of the probe sums.
+    __device__ long long pair_slices(int h, unsigned gen, int kind, const PairCtx& c) {
         Donation* r = &don->rec[h];
         long long sum = 0;
         for (;;) {
@@ -818,10 +852,10 @@ struct WarpCtx {
             lo = __shfl_sync(kFull, lo, 0);
             hi = __shfl_sync(kFull, hi, 0);
             if (hi <= lo) break;
-            sum += pair_pass(cand, lo, hi, bnd, T, cnt, ep, don_phase(kind));
+            sum += pair_run(c, kind, lo, hi);
             __syncwarp();
             if (lane == 0) {
-                __threadfence();  // the slice's table updates before its count
+                __threadfence();  // the slice's writes before its count
                 atomicAdd(&r->done, (unsigned)(hi - lo));
             }
         }
@@ -859,129 +893,121 @@ struct WarpCtx {
         return __shfl_sync(kFull, h, 0);
     }
 
-    // The pair sum with a dense counter array from the pool, shared with idle
-    // warps in three phases (count the fill side, sum over the probe side,
-    // zero the fill side's counters again), each finished by every helper
-    // before the next is published.  False (nothing done) when no array or
-    // no donation record is free.
-    __device__ bool pair_dense_shared(const int* candA, int na, const int* candB, int nb, int bnd, bool a_fills,
-                                      __int128& out) {
-        if (!dense || !don || split_min <= 0 || g.v_cnt > dense_words || na > 0xffffff || nb > 0xffffff) return false;
-        int slot = -1;
-        if (lane == 0) {
-            for (int i = 0; i < dense_slots && slot < 0; ++i) {
-                const int k = (int)((gw + i) % dense_slots);
-                if (atomicCAS(&dense_lock[k], 0u, 1u) == 0u) slot = k;
-            }
-        }
-        slot = __shfl_sync(kFull, slot, 0);
-        if (slot < 0) return false;
-        const int L1 = P->L - 1;
-        const int h = take_slot(L1 + 17);
-        if (h < 0) {
-            __syncwarp();
-            if (lane == 0) atomicExch(&dense_lock[slot], 0u);
-            __syncwarp();
-            return false;
-        }
-        unsigned* cnt = dense + (size_t)slot * (size_t)dense_words;
-        const int* fill = a_fills ? candA : candB;
-        const int nfill = a_fills ? na : nb;
-        const int* probe = a_fills ? candB : candA;
-        const int nprobe = a_fills ? nb : na;
-        const int fside = a_fills ? kDonSideA : 0, pside = a_fills ? 0 : kDonSideA;
-        long long sum = 0;
-        unsigned gen = pair_publish(h, kDonDenseFill | fside, nfill, 0u, slot);
-        pair_slices(h, gen, kDonDenseFill | fside, fill, bnd, nullptr, cnt, 0u);
-        pair_wait(h, nfill);
-        gen = pair_publish(h, kDonDenseProbe | pside, nprobe, 0u, slot);
-        sum += pair_slices(h, gen, kDonDenseProbe | pside, probe, bnd, nullptr, cnt, 0u);
-        pair_wait(h, nprobe);
-        gen = pair_publish(h, kDonDenseClear | fside, nfill, 0u, slot);
-        pair_slices(h, gen, kDonDenseClear | fside, fill, bnd, nullptr, cnt, 0u);
-        pair_wait(h, nfill);
+    __device__ void drop_slot(int h) {
+        if (h < 0) return;
         __syncwarp();
         if (lane == 0) {
             __threadfence();
-            atomicExch(&dense_lock[slot], 0u);
             atomicExch(&don->busy[h], 0u);
             atomicAdd(&don->held, ~0u);  // minus one
         }
         __syncwarp();
-        sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
-        out = lane == 0 ? (__int128)sum : (__int128)0;
-        return true;
+    }
+
+    // One phase over all of its units: shared through slot h, or by this
+    // warp alone when h < 0.
+    __device__ long long pair_phase(const PairCtx& c, int h, int kind, int units, unsigned tag, int aux) {
+        if (h < 0) return pair_run(c, kind, 0, units);
+        const unsigned gen = pair_publish(h, kind, units, tag, aux);
+        const long long sum = pair_slices(h, gen, kind, c);
+        pair_wait(h, units);
+        return sum;
     }
 
     // Sum over (v, w), v a level L-1 candidate, w a level L candidate, v != w,
-    // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c_x (the
-    // plan's pair_ok shape).  Level L-1's loop list is set.  Returns false
-    // (and does nothing) when the smaller side's neighbour lists would fill
-    // the table more than half: the caller then runs the level normally.
-    // A long pair sum is shared: idle warps take slices of the fill phase
-    // (inserting into this warp's table) and then of the probe phase (adding
-    // their sums to the pair's result), so one warp no longer carries a hub
-    // pair sum alone.
+    // of |N(v) ∩ N(w) ∩ [0, bound) \ chosen|, as sum_x a_x b_x - c (the
+    // plan's pair_ok shape; c the v == w terms).  Level L-1's loop list is
+    // set.  The smaller side (by list elements) counts its neighbours into
+    // this warp's hash table when it fills it at most half, else into a
+    // dense per-vertex counter array from the pool (zeroed again after);
+    // the other side sums the counts.  Long pair sums are shared with idle
+    // warps phase by phase (lengths, count, sum, zero).  Returns false (and
+    // counts nothing) when a dense array is needed and none is free, or the
+    // work is too long for one warp and no donation slot is free: the
+    // caller then runs the level normally.
     __device__ bool pair_level(__int128& out) {
+        constexpr long long kDenseMaxOps = 1ll << 24;  // one warp's longest dense pair sum
+        constexpr int kShareBlocks = GPM_PAIR_SHARE_BLOCKS;
         const int L1 = P->L - 1;
-        const int* candA;
-        const int* candB;
-        int na, nb, bnd;
-        pair_sides(candA, na, candB, nb, bnd);
-        // sizes of A's and B's neighbour lists below the bound; the smaller
-        // side fills the table, the other probes it (the sum is symmetric)
-        const long long ma = side_total(candA, na, bnd), mb = side_total(candB, nb, bnd);
-        if (c_pair_max_ops > 0 && ma + mb > c_pair_max_ops) return false;
-        const long long mins = min(ma, mb);
+        PairCtx c;
+        pair_ctx(c, gw);
+        out = 0;
+        if (c.na == 0 || c.nb == 0) return true;
+        const int nba = (c.na + 31) >> 5, nbb = (c.nb + 31) >> 5;
+        const bool can_share = don && split_min > 0 && nba + nbb <= 0xffffff;
+        int h = (can_share && nba + nbb >= kShareBlocks) ? take_slot(L1) : -1;
+        pair_phase(c, h, kDonPairLen, nba + nbb, 0u, c.na);
+        const unsigned ma = pair_scan(c.bsA, nba), mb = pair_scan(c.bsB, nbb);
+        if (ma == 0 || mb == 0) {
+            drop_slot(h);
+            return true;
+        }
+        const unsigned long long total = (unsigned long long)ma + mb;
+        if (c_pair_max_ops > 0 && (long long)total > c_pair_max_ops) {
+            drop_slot(h);
+            return false;
+        }
+        if (h < 0 && can_share && total >= 64ull * (unsigned long long)split_min) h = take_slot(L1);
         const bool a_fills = ma < mb;
-        if (mins * 2 > (long long)pmask + 1) {
-            // too big for the table: a dense counter array, shared with idle
-            // warps when loops are shared, else one warp for bounded work
-            if (pair_dense_shared(candA, na, candB, nb, bnd, a_fills, out)) return true;
-            return pair_level_dense(candA, na, candB, nb, bnd, a_fills, ma + mb + mins, out);
-        }
-        __syncwarp();
-        if (lane == 0) {
-            s->epoch = (s->epoch + 1) & 0xffffu;
-            if (s->epoch == 0) s->epoch = 1;
-        }
-        __syncwarp();
-        const unsigned ep = s->epoch;
-        if (ep == 1) {  // fresh cycle of tags: clear the table
-            for (unsigned i = lane; i <= pmask; i += 32) ptab[i] = 0ull;
+        const unsigned mins = a_fills ? ma : mb, maxs = a_fills ? mb : ma;
+        int dslot = -1;
+        unsigned tag;
+        if (2ull * mins > (unsigned long long)pmask + 1ull) {
+            // too big for the table: a dense counter array
+            if (!dense || g.v_cnt > dense_words || (h < 0 && (long long)(total + mins) > kDenseMaxOps)) {
+                drop_slot(h);
+                return false;
+            }
+            if (lane == 0) {
+                for (int i = 0; i < dense_slots && dslot < 0; ++i) {
+                    const int k = (int)((gw + i) % dense_slots);
+                    if (atomicCAS(&dense_lock[k], 0u, 1u) == 0u) dslot = k;
+                }
+            }
+            dslot = __shfl_sync(kFull, dslot, 0);
+            if (dslot < 0) {
+                drop_slot(h);
+                return false;
+            }
+            c.cnt = dense + (size_t)dslot * (size_t)dense_words;
+            tag = (unsigned)dslot;
+        } else {
             __syncwarp();
+            if (lane == 0) {
+                s->epoch = (s->epoch + 1) & 0xffffu;
+                if (s->epoch == 0) s->epoch = 1;
+            }
+            __syncwarp();
+            c.ep = s->epoch;
+            c.T = ptab;
+            if (c.ep == 1) {  // fresh cycle of tags: clear the table
+                for (unsigned i = lane; i <= pmask; i += 32) ptab[i] = 0ull;
+                __syncwarp();
+            }
+            tag = c.ep;
         }
-        const int* fill = a_fills ? candA : candB;
-        const int nfill = a_fills ? na : nb;
-        const int* probe = a_fills ? candB : candA;
-        const int nprobe = a_fills ? nb : na;
+        // element units: 2^GPM_PAIR_UNIT_LOG2 elements, coarser when a side
+        // would exceed 2^24 units
+        int ul = GPM_PAIR_UNIT_LOG2;
+        while (((unsigned long long)maxs >> ul) >= 0xffffffull) ++ul;
+        const unsigned long long um = (1ull << ul) - 1;
+        const int ufill = (int)((mins + um) >> ul), uprobe = (int)((maxs + um) >> ul);
+        const int fside = a_fills ? kDonSideA : 0, pside = a_fills ? 0 : kDonSideA;
+        const int nfill = a_fills ? c.na : c.nb, nprobe = a_fills ? c.nb : c.na;
+        const int kf = c.cnt ? kDonDenseFill : kDonPairFill, kp = c.cnt ? kDonDenseProbe : kDonPairProbe;
         long long sum = 0;
-        const int h = (don && split_min > 0 && ma + mb >= 64ll * split_min && nfill <= 0xffffff && nprobe <= 0xffffff)
-                          ? take_slot(L1)
-                          : -1;
-        if (h >= 0) {
-            const int fill_kind = kDonPairFill | (a_fills ? kDonSideA : 0);
-            const int probe_kind = kDonPairProbe | (a_fills ? 0 : kDonSideA);
-            unsigned gen = pair_publish(h, fill_kind, nfill, ep, (int)gw);
-            pair_slices(h, gen, fill_kind, fill, bnd, ptab, nullptr, ep);
-            pair_wait(h, nfill);
-            gen = pair_publish(h, probe_kind, nprobe, ep, (int)gw);
-            sum += pair_slices(h, gen, probe_kind, probe, bnd, ptab, nullptr, ep);
-            pair_wait(h, nprobe);
+        pair_phase(c, h, kf | fside | (ul << 16), ufill, tag, nfill);
+        sum += pair_phase(c, h, kp | pside | (ul << 16), uprobe, tag, nprobe);
+        if (c.cnt) pair_phase(c, h, kDonDenseClear | fside | (ul << 16), ufill, tag, nfill);
+        drop_slot(h);
+        if (dslot >= 0) {
             __syncwarp();
             if (lane == 0) {
                 __threadfence();
-                atomicExch(&don->busy[h], 0u);
-                atomicAdd(&don->held, ~0u);  // minus one
+                atomicExch(&dense_lock[dslot], 0u);
             }
             __syncwarp();
-        } else {
-            pair_pass(fill, 0, nfill, bnd, ptab, nullptr, ep, 0);
-            sum += pair_pass(probe, 0, nprobe, bnd, ptab, nullptr, ep, 1);
         }
-        sum -= pair_c_term(candA, na, candB, nb, bnd, L1);
 #pragma unroll
         for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
         out = lane == 0 ? (__int128)sum : (__int128)0;
@@ -1345,23 +1371,62 @@ struct WarpCtx {
         __syncwarp();
     }
 
-    // next slice of the donated loop at depth d into idx[d], end[d]
+    // Next slice of the donated loop at depth d into idx[d], end[d].  A loop
+    // slice is weighted: its candidates' neighbour lists (their degrees, the
+    // cost of the intersections below them) add up to at most kLoopBudget
+    // elements, or it is one candidate.  Loop lists run in id order, which is
+    // descending degree, so the hubs at a loop's start come one per slice
+    // instead of 64 to the first claimer.
     __device__ bool claim_more(int d) {
-        int lo = 0, hi = 0;
+        constexpr unsigned kLoopBudget = 16384;
         __syncwarp();
         if ((unsigned)s->dslot[d] >= (unsigned)kDonSlots) {
             if (lane == 0) record_check(kErrDonation, d, s->dslot[d], 0, 0, 0, 1);
             return false;
         }
-        if (lane == 0) {
-            don_claim(&don->rec[s->dslot[d]], s->dgen[d], (d == P->L && batch_on()) ? kDonLeaf : kDonLoop, lo, hi);
-            if (hi > lo) {
-                s->idx[d] = lo;
-                s->end[d] = hi;
+        Donation* r = &don->rec[s->dslot[d]];
+        const unsigned gen = s->dgen[d] & 0xffffu;
+        const bool leaf = d == P->L && batch_on();
+        const int* list = s->lp[d];
+        int lo = 0, hi = 0;
+        for (int tries = 0; tries < (1 << 24); ++tries) {
+            unsigned long long w = 0;
+            if (lane == 0) w = *(volatile unsigned long long*)&r->word;
+            w = __shfl_sync(kFull, w, 0);
+            const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
+            if ((unsigned)(w >> 48) != gen || next >= end) break;
+            const unsigned smin = leaf ? 8u : 1u, smax = leaf ? 128u : 64u;
+            unsigned take = min(end - next, min(smax, max(smin, (end - next) >> 5)));
+            if (!leaf) {
+                const unsigned look = min(take, 32u);
+                unsigned dg = 0;
+                if ((unsigned)lane < look) {
+                    const int v = list[next + lane];
+                    dg = g.rowptr[v + 1] - g.rowptr[v];
+                }
+                unsigned incl = dg;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned t = __shfl_up_sync(kFull, incl, o);
+                    if (lane >= o) incl += t;
+                }
+                const unsigned fit = __popc(__ballot_sync(kFull, (unsigned)lane < look && incl <= kLoopBudget));
+                if (fit < look) take = max(1u, fit);
+            }
+            unsigned long long got = 0;
+            if (lane == 0) got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
+            got = __shfl_sync(kFull, got, 0);
+            if (got == w) {
+                lo = (int)next;
+                hi = (int)(next + take);
+                break;
             }
         }
-        hi = __shfl_sync(kFull, hi, 0);
-        lo = __shfl_sync(kFull, lo, 0);
+        __syncwarp();
+        if (lane == 0 && hi > lo) {
+            s->idx[d] = lo;
+            s->end[d] = hi;
+        }
         __syncwarp();
         return hi > lo;
     }
@@ -1481,7 +1546,7 @@ struct WarpCtx {
     // false when nothing could be taken.
     __device__ bool help_one(const PairDesc* pairs, int npairs, unsigned long long* out, int h, unsigned gen) {
         Donation* r = &don->rec[h];
-        int lo = 0, hi = 0, p = 0, d = 0, rend = 0, kind = 0, owner_w = 0;
+        int lo = 0, hi = 0, p = 0, d = 0, rend = 0, kind = 0, owner_w = 0, aux = 0;
         unsigned ep = 0;
         if (lane == 0) {
             const unsigned long long w = *(volatile unsigned long long*)&r->word;
@@ -1494,6 +1559,7 @@ struct WarpCtx {
                 kind = vr->kind;
                 owner_w = vr->owner;
                 ep = vr->epoch;
+                aux = vr->chosen[kMaxN - 1];
                 rend = (int)((w >> 24) & 0xffffffu);
                 // the claim succeeds only while the record still holds these fields
                 don_claim(r, gen, kind, lo, hi);
@@ -1507,12 +1573,17 @@ struct WarpCtx {
         kind = __shfl_sync(kFull, kind, 0);
         owner_w = __shfl_sync(kFull, owner_w, 0);
         ep = __shfl_sync(kFull, ep, 0);
+        aux = __shfl_sync(kFull, aux, 0);
         __syncwarp();
         if (hi <= lo) return false;
         const bool pair_kind = don_pair_kind(kind);
         const bool dense_kind = don_dense_kind(kind);
-        const bool bad_owner = pair_kind && (dense_kind ? (!dense || (unsigned)owner_w >= (unsigned)dense_slots)
-                                                       : (!ptab_base || (unsigned)owner_w >= gridDim.x * (blockDim.x >> 5)));
+        const bool len_kind = (kind & 0xff) == kDonPairLen;
+        // pair sums: the owner's warp index locates its arrays (and table);
+        // a dense phase's tag is its counter array
+        const bool bad_owner =
+            pair_kind && ((unsigned)owner_w >= gridDim.x * (blockDim.x >> 5) ||
+                          (dense_kind ? (!dense || ep >= (unsigned)dense_slots) : (!len_kind && !ptab_base)));
         if (p < 0 || p >= npairs || bad_owner) {
             if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
             __syncwarp();
@@ -1531,17 +1602,12 @@ struct WarpCtx {
             ok = build_chain(l, nv, dv);
         }
         if (ok) start_level(d);
-        const int* cand = nullptr;
-        int bnd = 0;
+        PairCtx pc;
         if (ok && pair_kind) {
-            // the phase's side of the owner's pair sum, as the owner chose it
-            const int* candA;
-            const int* candB;
-            int na, nb;
-            pair_sides(candA, na, candB, nb, bnd);
-            const bool use_a = (kind & kDonSideA) != 0;
-            cand = use_a ? candA : candB;
-            ok = (use_a ? na : nb) == rend;
+            // the owner's pair sum as this warp rebuilds it: the same lists
+            pair_ctx(pc, owner_w);
+            if (len_kind) ok = aux == pc.na && rend == ((pc.na + 31) >> 5) + ((pc.nb + 31) >> 5);
+            else ok = aux == ((kind & kDonSideA) ? pc.na : pc.nb);
         } else if (ok) {
             ok = s->end[d] == rend;
         }
@@ -1552,20 +1618,24 @@ struct WarpCtx {
             return true;
         }
         if (pair_kind) {
-            unsigned long long* T = dense_kind ? nullptr : ptab_base + ((size_t)owner_w << pair_log2);
-            unsigned* cnt = dense_kind ? dense + (size_t)owner_w * (size_t)dense_words : nullptr;
-            if (dense_kind && g.v_cnt > dense_words) {
-                if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, -3);
-                __syncwarp();
-                return true;
+            if (dense_kind) {
+                if (g.v_cnt > dense_words) {
+                    if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, -3);
+                    __syncwarp();
+                    return true;
+                }
+                pc.cnt = dense + (size_t)ep * (size_t)dense_words;
+            } else if (!len_kind) {
+                pc.T = ptab_base + ((size_t)owner_w << pair_log2);
+                pc.ep = ep;
             }
-            long long sum = pair_pass(cand, lo, hi, bnd, T, cnt, ep, don_phase(kind));
+            long long sum = pair_run(pc, kind, lo, hi);
             __syncwarp();
             if (lane == 0) {
                 __threadfence();
                 atomicAdd(&r->done, (unsigned)(hi - lo));
             }
-            sum += pair_slices(h, gen, kind, cand, bnd, T, cnt, ep);
+            sum += pair_slices(h, gen, kind, pc);
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
             if (lane == 0 && sum != 0) add128(out + 2 * p, (__int128)sum);
@@ -1700,6 +1770,7 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : (kMinBlocks == 5 ? 128
     w.pair_log2 = pair_log2;
     if (lane == 0) w.s->epoch = 0;  // the first pair sum clears the table
     w.scratch = scratch_all + gw * scratch_per_warp;
+    w.spw = scratch_per_warp;
     w.lane = lane;
     w.bytes = 0;
     w.don = don;

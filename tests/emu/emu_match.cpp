@@ -121,7 +121,9 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     int nslots = 1;
     for (const Sched& s : ss) nslots = std::max(nslots, s.plan.nslots);
     const int cap = std::max(1, g.max_deg) + kGuard;  // slot stride; the last kGuard ints are poisoned
-    const long long per_warp = (long long)nslots * cap + kGuard;
+    // slots, a poisoned guard, then the pair sums' block-sum tail (the
+    // kernel finds the tail at the end of each warp's region)
+    const long long per_warp = (long long)nslots * cap + kGuard + 2 * pair_bs_stride(cap);
     const int warps = k.blocks * k.wpb;
     std::vector<int> scratch((size_t)warps * per_warp);
     for (int w = 0; w < warps; ++w) {
@@ -336,6 +338,29 @@ void case_pair() {
         }
 }
 
+// hubs: candidate lists of hundreds of vertices, so that the list lengths
+// are computed as a shared phase and the element phases run in many slices
+// of a few units each
+void case_pairhub() {
+    const Csr g = chung_lu(600, 8.0, 2.1, 250, 14);
+    std::vector<Sched> ss;
+    for (const Sched& s : motif_schedules(g, 5, true, 1))
+        if (s.plan.pair_ok) ss.push_back(s);
+    if (ss.empty()) {
+        std::printf("no pair-sum plan\n");
+        ++failures;
+        return;
+    }
+    for (int log2 : {13, 6}) {  // the hash table, and dense arrays for the big sums
+        Knobs k;
+        k.pair = 1;
+        k.split = 1;
+        k.pair_log2 = log2;
+        k.dense = 2;
+        expect_oracle("pair-sum hubs", g, ss, k);
+    }
+}
+
 void case_stripes() {
     const Csr g = rmat(8, 10, 8);
     std::vector<Sched> ss = motif_schedules(g, 4, true, 1);
@@ -378,12 +403,13 @@ void case_stripes() {
 int main(int argc, char** argv) {
     std::vector<std::string> cases;
     for (int i = 1; i < argc; ++i) cases.push_back(argv[i]);
-    if (cases.empty()) cases = {"quick", "pair", "stripes", "vec"};
+    if (cases.empty()) cases = {"quick", "pair", "pairhub", "stripes", "vec"};
     for (const std::string& c : cases) {
         if (c == "quick") case_quick();
         else if (c == "donation") case_donation();
         else if (c == "leafslices") case_leafslices();
         else if (c == "pair") case_pair();
+        else if (c == "pairhub") case_pairhub();
         else if (c == "stripes") case_stripes();
         else if (c == "vec") case_vec();
         else {

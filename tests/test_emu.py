@@ -4,7 +4,8 @@ AddressSanitizer, run on small skewed graphs and compared with the oracle.
 
 Covers, without a GPU: loop donation with every loop shared (split=1, the
 most racy setting) with and without the batched leaf, the pair-sum leaf and
-its dense counter arrays, leaf bitmaps, stripes that do not depend on the
+its dense counter arrays (every phase shared, in one-element slices), leaf
+bitmaps, stripes that do not depend on the
 grab size and that add up to the whole job (the multi-rank split); any
 out-of-bounds access, any lane that meets a different shuffle/ballot/syncwarp
 than its warp, and any internal check stops the run."""
@@ -27,7 +28,10 @@ INCLUDES = [f"-I{ROOT / 'include'}", f"-I{CSRC}", f"-I{EMU}"]
 
 def _build() -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
-    jobs = [(["g++", "-std=c++20", *FLAGS, *INCLUDES, "-c", str(EMU / "emu_match.cpp"), "-o", str(OUT / "emu.o")])]
+    # pair sums shared from one block of candidates on, in one-element units
+    stress = ["-DGPM_PAIR_SHARE_BLOCKS=1", "-DGPM_PAIR_UNIT_LOG2=0"]
+    jobs = [(["g++", "-std=c++20", *FLAGS, *stress, *INCLUDES, "-c", str(EMU / "emu_match.cpp"),
+              "-o", str(OUT / "emu.o")])]
     for src in HOST_SOURCES:
         jobs.append(["g++", "-std=c++17", *FLAGS, "-DGPM_HOST_ONLY", *INCLUDES, "-c", str(CSRC / src),
                      "-o", str(OUT / (src + ".o"))])
@@ -47,7 +51,7 @@ def _build() -> Path:
 def test_device_core_on_emulated_warps():
     exe = _build()
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
-    r = subprocess.run([str(exe), "quick", "pair", "stripes", "vec"], capture_output=True, text=True, timeout=900, env=env)
+    r = subprocess.run([str(exe), "quick", "pair", "pairhub", "stripes", "vec"], capture_output=True, text=True, timeout=900, env=env)
     tail = (r.stdout[-3000:] + "\n" + r.stderr[-3000:]).strip()
     assert r.returncode == 0, tail
     assert "PASSED (0 mismatches)" in r.stdout, tail
