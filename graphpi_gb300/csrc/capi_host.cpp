@@ -672,6 +672,7 @@ GPM_API int gpm_set_option(const char* key, int64_t value) {
     else if (k == "stage_tma") slot = &o.stage_tma, lo = 0, hi = 1;
     else if (k == "schedule_gpu") slot = &o.schedule_gpu, lo = 0, hi = 1;
     else if (k == "merge_vec") slot = &o.merge_vec, lo = 0, hi = 1;
+    else if (k == "pool") slot = &o.pool, lo = 0, hi = 1;
     else if (k == "leaf_batch") slot = &o.leaf_batch, lo = 0, hi = 1;
     else if (k == "pair_leaf") slot = &o.pair_leaf, lo = 0, hi = 1;
     else if (k == "pair_log2") slot = &o.pair_log2, lo = 0, hi = 24;
@@ -718,6 +719,7 @@ GPM_API int gpm_get_option(const char* key, int64_t* value) {
     else if (k == "stage_tma") *value = o.stage_tma;
     else if (k == "schedule_gpu") *value = o.schedule_gpu;
     else if (k == "merge_vec") *value = o.merge_vec;
+    else if (k == "pool") *value = o.pool;
     else if (k == "leaf_batch") *value = o.leaf_batch;
     else if (k == "pair_leaf") *value = o.pair_leaf;
     else if (k == "pair_log2") *value = o.pair_log2;

@@ -289,6 +289,7 @@ struct DeviceCtx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
+    cudaMemPool_t pool = nullptr;  // graph arrays and construction temporaries (null: cudaMalloc)
     std::mutex mu;
 };
 
@@ -326,6 +327,26 @@ static DeviceCtx* get_ctx(int* err) {
             *err = GPM_ERR_CUDA;
             return nullptr;
         }
+        // A stream-ordered pool that keeps freed memory (up to a quarter of
+        // the device) for the next call, so that a graph uploaded per call
+        // does not map and unmap its buffers every time.  Without it (an
+        // error here, or option pool=0) buffers come from cudaMalloc.
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = t_device;
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && cudaMemPoolCreate(&nc->pool, &props) == cudaSuccess) {
+            unsigned long long keep = (unsigned long long)(total_b / 4);
+            if (cudaMemPoolSetAttribute(nc->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+                cudaMemPoolDestroy(nc->pool);
+                nc->pool = nullptr;
+            }
+        } else {
+            nc->pool = nullptr;
+        }
+        cudaGetLastError();
         c = nc;
     }
     if (cudaSetDevice(t_device) != cudaSuccess) {
@@ -348,12 +369,46 @@ static int ensure_scratch(DeviceCtx* c, size_t bytes) {
 }
 
 // RAII device buffer for one call
+static bool use_pool(const DeviceCtx* c) { return c->pool != nullptr && options().pool != 0; }
+
+static cudaError_t buf_alloc(DeviceCtx* c, void** p, size_t bytes, bool pooled) {
+    return pooled ? cudaMallocFromPoolAsync(p, bytes, c->pool, c->stream) : cudaMalloc(p, bytes);
+}
+
+// frees a buffer of buf_alloc (stream-ordered on the context's stream when pooled)
+static void buf_free(void* p, bool pooled, cudaStream_t st) {
+    if (!p) return;
+    if (pooled) cudaFreeAsync(p, st);
+    else cudaFree(p);
+}
+
 struct DevBuf {
     void* p = nullptr;
-    ~DevBuf() {
-        if (p) cudaFree(p);
+    bool pooled = false;
+    cudaStream_t st = nullptr;
+    cudaError_t alloc(DeviceCtx* c, size_t bytes) { return alloc(c, bytes, use_pool(c)); }
+    cudaError_t alloc(DeviceCtx* c, size_t bytes, bool from_pool) {
+        pooled = from_pool;
+        st = c->stream;
+        return buf_alloc(c, &p, bytes, pooled);
     }
+    ~DevBuf() { buf_free(p, pooled, st); }
 };
+
+// The graph's device arrays.  With pooled arrays the device is synchronised
+// first, as cudaFree would: no kernel on any stream reads them any more.
+static void graph_free_arrays(gpm_graph* g) {
+    void* ps[4] = {g->orig_rowptr != g->rowptr ? (void*)g->orig_rowptr : nullptr,
+                   g->orig_col != g->col ? (void*)g->orig_col : nullptr, g->rowptr, g->col};
+    if (g->pooled) cudaDeviceSynchronize();
+    for (void* q : ps) buf_free(q, g->pooled, (cudaStream_t)g->stream);
+    g->orig_rowptr = g->rowptr = nullptr;
+    g->orig_col = g->col = nullptr;
+}
+
+static cudaError_t graph_alloc(DeviceCtx* c, gpm_graph* g, void** p, size_t bytes) {
+    return buf_alloc(c, p, bytes, g->pooled);
+}
 
 // Reports (and clears) an internal-check record left by a kernel.
 static int take_check(const char* where) {
@@ -376,17 +431,17 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     const unsigned E = (unsigned)g->e_cnt;
     cudaStream_t st = c->stream;
     DevBuf keys, keys2, ids, order, tmp;
-    GPM_CK(cudaMalloc(&keys.p, sizeof(unsigned) * (size_t)std::max(V, 1)));
-    GPM_CK(cudaMalloc(&keys2.p, sizeof(unsigned) * (size_t)std::max(V, 1)));
-    GPM_CK(cudaMalloc(&ids.p, sizeof(int) * (size_t)std::max(V, 1)));
-    GPM_CK(cudaMalloc(&order.p, sizeof(int) * (size_t)std::max(V, 1)));
+    GPM_CK(keys.alloc(c, sizeof(unsigned) * (size_t)std::max(V, 1)));
+    GPM_CK(keys2.alloc(c, sizeof(unsigned) * (size_t)std::max(V, 1)));
+    GPM_CK(ids.alloc(c, sizeof(int) * (size_t)std::max(V, 1)));
+    GPM_CK(order.alloc(c, sizeof(int) * (size_t)std::max(V, 1)));
     const int threads = 256, blocks = c->num_sms * 8;
     degree_keys_kernel<<<blocks, threads, 0, st>>>(g->rowptr, V, (unsigned*)keys.p, (int*)ids.p);
     GPM_CK(cudaGetLastError());
     size_t tb = 0;
     GPM_CK(cub::DeviceRadixSort::SortPairs(nullptr, tb, (unsigned*)keys.p, (unsigned*)keys2.p, (int*)ids.p,
                                            (int*)order.p, V, 0, 32, st));
-    GPM_CK(cudaMalloc(&tmp.p, std::max<size_t>(tb, 1)));
+    GPM_CK(tmp.alloc(c, std::max<size_t>(tb, 1)));
     GPM_CK(cub::DeviceRadixSort::SortPairs(tmp.p, tb, (unsigned*)keys.p, (unsigned*)keys2.p, (int*)ids.p,
                                            (int*)order.p, V, 0, 32, st));
     unsigned top[2] = {~0u, ~0u};
@@ -397,17 +452,17 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     if (!relabel || V == 0 || E == 0) return GPM_OK;
 
     DevBuf new_id, new_deg, new_rowptr, new_col_u, new_col, tmp2;
-    GPM_CK(cudaMalloc(&new_id.p, sizeof(int) * (size_t)V));
-    GPM_CK(cudaMalloc(&new_deg.p, sizeof(unsigned) * ((size_t)V + 1)));
-    GPM_CK(cudaMalloc(&new_rowptr.p, sizeof(unsigned) * ((size_t)V + 1)));
-    GPM_CK(cudaMalloc(&new_col_u.p, sizeof(int) * (size_t)E));
-    GPM_CK(cudaMalloc(&new_col.p, sizeof(int) * (size_t)E + kCsrSlack));
+    GPM_CK(new_id.alloc(c, sizeof(int) * (size_t)V));
+    GPM_CK(new_deg.alloc(c, sizeof(unsigned) * ((size_t)V + 1)));
+    GPM_CK(new_rowptr.alloc(c, sizeof(unsigned) * ((size_t)V + 1), g->pooled));
+    GPM_CK(new_col_u.alloc(c, sizeof(int) * (size_t)E));
+    GPM_CK(new_col.alloc(c, sizeof(int) * (size_t)E + kCsrSlack, g->pooled));
     relabel_maps_kernel<<<blocks, threads, 0, st>>>(g->rowptr, (const int*)order.p, V, (int*)new_id.p,
                                                     (unsigned*)new_deg.p);
     GPM_CK(cudaGetLastError());
     size_t sb = 0;
     GPM_CK(cub::DeviceScan::ExclusiveSum(nullptr, sb, (unsigned*)new_deg.p, (unsigned*)new_rowptr.p, V + 1, st));
-    GPM_CK(cudaMalloc(&tmp2.p, std::max<size_t>(sb, 1)));
+    GPM_CK(tmp2.alloc(c, std::max<size_t>(sb, 1)));
     GPM_CK(cub::DeviceScan::ExclusiveSum(tmp2.p, sb, (unsigned*)new_deg.p, (unsigned*)new_rowptr.p, V + 1, st));
     relabel_fill_kernel<<<blocks, threads, 0, st>>>(g->rowptr, g->col, (const int*)order.p, (const int*)new_id.p,
                                                     (const unsigned*)new_rowptr.p, V, (int*)new_col_u.p);
@@ -416,7 +471,7 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     GPM_CK(cub::DeviceSegmentedSort::SortKeys(nullptr, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
                                               (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
     DevBuf tmp3;
-    GPM_CK(cudaMalloc(&tmp3.p, std::max<size_t>(ssb, 1)));
+    GPM_CK(tmp3.alloc(c, std::max<size_t>(ssb, 1)));
     GPM_CK(cub::DeviceSegmentedSort::SortKeys(tmp3.p, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
                                               (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
     GPM_CK(cudaStreamSynchronize(st));
@@ -446,19 +501,19 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
 }
 
 static unsigned validate_csr(DeviceCtx* c, const GraphView& v, int* rc) {
-    unsigned long long* d_words = nullptr;
+    DevBuf buf;
     unsigned long long w[5] = {0, 0, 0, 0, 0};
     *rc = GPM_OK;
-    if (cudaMalloc(&d_words, sizeof w) != cudaSuccess) {
+    if (buf.alloc(c, sizeof w) != cudaSuccess) {
         set_error("validate: out of device memory");
         *rc = GPM_ERR_OOM;
         return 0;
     }
+    unsigned long long* d_words = (unsigned long long*)buf.p;
     cudaMemsetAsync(d_words, 0, sizeof w, c->stream);
     validate_kernel<<<c->num_sms * 8, 256, 0, c->stream>>>(v, d_words);
     cudaMemcpyAsync(w, d_words, sizeof w, cudaMemcpyDeviceToHost, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
-    cudaFree(d_words);
     if (e != cudaSuccess) {
         set_error("validate: %s", cudaGetErrorString(e));
         *rc = GPM_ERR_CUDA;
@@ -718,9 +773,9 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     rc = ensure_scratch(c, scratch_bytes(ls));
     if (rc) return rc;
     DevBuf d_pairs, d_small;
-    GPM_CK(cudaMalloc(&d_pairs.p, sizeof(PairDesc) * n));
+    GPM_CK(d_pairs.alloc(c, sizeof(PairDesc) * n));
     const size_t words = small_words(n);
-    GPM_CK(cudaMalloc(&d_small.p, words * sizeof(unsigned long long)));
+    GPM_CK(d_small.alloc(c, words * sizeof(unsigned long long)));
     cudaStream_t st = c->stream;
     std::vector<unsigned long long> init(words, 0);
     init[3 * n + 2] = (unsigned long long)options().stripes;
@@ -775,7 +830,7 @@ static int finish_graph(DeviceCtx* c, gpm_graph* g, bool relabel, const char* wh
     cudaStream_t st = c->stream;
     DevBuf d_words;
     unsigned long long w[5] = {0, 0, 0, 0, 0};
-    GPM_CK(cudaMalloc(&d_words.p, sizeof w));
+    GPM_CK(d_words.alloc(c, sizeof w));
     GPM_CK(cudaMemsetAsync(d_words.p, 0, sizeof w, st));
     validate_kernel<<<c->num_sms * 8, 256, 0, st>>>(view_of(g), (unsigned long long*)d_words.p);
     GPM_CK(cudaMemcpyAsync(w, d_words.p, sizeof w, cudaMemcpyDeviceToHost, st));
@@ -832,17 +887,16 @@ GPM_API int gpm_graph_create(int32_t v_cnt, const uint32_t* rowptr, const int32_
     g->v_cnt = v_cnt;
     g->e_cnt = E;
     g->device = c->device;
+    g->pooled = use_pool(c);
+    g->stream = c->stream;
     auto fail = [&](int rc) {
-        if (g->orig_rowptr && g->orig_rowptr != g->rowptr) cudaFree(g->orig_rowptr);
-        if (g->orig_col && g->orig_col != g->col) cudaFree(g->orig_col);
-        if (g->rowptr) cudaFree(g->rowptr);
-        if (g->col) cudaFree(g->col);
+        graph_free_arrays(g);
         delete g;
         return rc;
     };
     cudaStream_t st = c->stream;
-    if (cudaMalloc(&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
-        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(E, 1) + kCsrSlack) != cudaSuccess) {
+    if (graph_alloc(c, g, (void**)&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
+        graph_alloc(c, g, (void**)&g->col, sizeof(int32_t) * std::max<size_t>(E, 1) + kCsrSlack) != cudaSuccess) {
         set_error("gpm_graph_create: out of device memory for %llu edges", (unsigned long long)E);
         return fail(GPM_ERR_OOM);
     }
@@ -915,13 +969,13 @@ GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, c
     cudaStream_t st = c->stream;
     const size_t n2 = (size_t)std::max<int64_t>(1, 2 * m);
     DevBuf d_src, d_dst, keys, keys2, uniq, nsel, bad, tmp;
-    GPM_CK(cudaMalloc(&d_src.p, sizeof(int) * std::max<int64_t>(m, 1)));
-    GPM_CK(cudaMalloc(&d_dst.p, sizeof(int) * std::max<int64_t>(m, 1)));
-    GPM_CK(cudaMalloc(&keys.p, sizeof(unsigned long long) * n2));
-    GPM_CK(cudaMalloc(&keys2.p, sizeof(unsigned long long) * n2));
-    GPM_CK(cudaMalloc(&uniq.p, sizeof(unsigned long long) * n2));
-    GPM_CK(cudaMalloc(&nsel.p, sizeof(unsigned long long)));
-    GPM_CK(cudaMalloc(&bad.p, sizeof(unsigned)));
+    GPM_CK(d_src.alloc(c, sizeof(int) * std::max<int64_t>(m, 1)));
+    GPM_CK(d_dst.alloc(c, sizeof(int) * std::max<int64_t>(m, 1)));
+    GPM_CK(keys.alloc(c, sizeof(unsigned long long) * n2));
+    GPM_CK(keys2.alloc(c, sizeof(unsigned long long) * n2));
+    GPM_CK(uniq.alloc(c, sizeof(unsigned long long) * n2));
+    GPM_CK(nsel.alloc(c, sizeof(unsigned long long)));
+    GPM_CK(bad.alloc(c, sizeof(unsigned)));
     GPM_CK(cudaMemsetAsync(bad.p, 0, sizeof(unsigned), st));
     if (m > 0) {
         GPM_CK(cudaMemcpyAsync(d_src.p, src, sizeof(int) * m, cudaMemcpyHostToDevice, st));
@@ -936,7 +990,7 @@ GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, c
                                           n2i, 0, 64, st));
     GPM_CK(cub::DeviceSelect::Unique(nullptr, tb_uniq, (unsigned long long*)keys2.p, (unsigned long long*)uniq.p,
                                      (unsigned long long*)nsel.p, n2i, st));
-    GPM_CK(cudaMalloc(&tmp.p, std::max<size_t>(std::max(tb_sort, tb_uniq), 1)));
+    GPM_CK(tmp.alloc(c, std::max<size_t>(std::max(tb_sort, tb_uniq), 1)));
     unsigned long long h_n = 0, h_last = ~0ull;
     unsigned h_bad = 0;
     if (m > 0) {
@@ -960,9 +1014,11 @@ GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, c
     g->v_cnt = v_cnt;
     g->e_cnt = h_n;
     g->device = c->device;
-    if (cudaMalloc(&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
-        cudaMalloc(&g->col, sizeof(int32_t) * std::max<size_t>(h_n, 1) + kCsrSlack) != cudaSuccess) {
-        if (g->rowptr) cudaFree(g->rowptr);
+    g->pooled = use_pool(c);
+    g->stream = c->stream;
+    if (graph_alloc(c, g, (void**)&g->rowptr, sizeof(uint32_t) * ((size_t)v_cnt + 1)) != cudaSuccess ||
+        graph_alloc(c, g, (void**)&g->col, sizeof(int32_t) * std::max<size_t>(h_n, 1) + kCsrSlack) != cudaSuccess) {
+        graph_free_arrays(g);
         delete g;
         set_error("gpm_graph_from_edges: out of device memory for %llu edges", h_n);
         return GPM_ERR_OOM;
@@ -971,10 +1027,7 @@ GPM_API int gpm_graph_from_edges(int32_t v_cnt, int64_t m, const int32_t* src, c
                                                        g->col);
     const int rc = finish_graph(c, g, relabel != 0, "gpm_graph_from_edges");
     if (rc) {
-        if (g->orig_rowptr && g->orig_rowptr != g->rowptr) cudaFree(g->orig_rowptr);
-        if (g->orig_col && g->orig_col != g->col) cudaFree(g->orig_col);
-        cudaFree(g->rowptr);
-        cudaFree(g->col);
+        graph_free_arrays(g);
         delete g;
         return rc;
     }
@@ -1014,10 +1067,7 @@ GPM_API int gpm_graph_destroy(gpm_graph* g) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaSetDevice(g->device);
-    if (g->orig_rowptr && g->orig_rowptr != g->rowptr) cudaFree(g->orig_rowptr);
-    if (g->orig_col && g->orig_col != g->col) cudaFree(g->orig_col);
-    if (g->rowptr) cudaFree(g->rowptr);
-    if (g->col) cudaFree(g->col);
+    graph_free_arrays(g);
     cudaSetDevice(dev);
     delete g;
     return GPM_OK;
@@ -1048,7 +1098,7 @@ GPM_API int gpm_tri_count(gpm_graph* g, uint64_t* out) {
     if (!c) return err;
     std::lock_guard<std::mutex> lk(c->mu);
     DevBuf buf;
-    GPM_CK(cudaMalloc(&buf.p, 2 * sizeof(unsigned long long)));
+    GPM_CK(buf.alloc(c, 2 * sizeof(unsigned long long)));
     cudaStream_t st = c->stream;
     GPM_CK(cudaMemsetAsync(buf.p, 0, 2 * sizeof(unsigned long long), st));
     unsigned long long* d = (unsigned long long*)buf.p;
@@ -1089,7 +1139,7 @@ GPM_API int gpm_clique_count(gpm_graph* g, int32_t k, gpm_u128* out) {
     if (rc) return rc;
     DevBuf buf;
     // cursor, 128-bit count, stripes, stripe
-    GPM_CK(cudaMalloc(&buf.p, 5 * sizeof(unsigned long long)));
+    GPM_CK(buf.alloc(c, 5 * sizeof(unsigned long long)));
     cudaStream_t st = c->stream;
     const unsigned long long init[5] = {0, 0, 0, (unsigned long long)std::max<int64_t>(1, o.stripes),
                                         (unsigned long long)o.stripe};

@@ -35,6 +35,7 @@ struct Options {
     int64_t stripe = 0;
     int64_t raw_sums = 0;       // 1: return undivided 128-bit sums
     int64_t merge_vec = 1;      // 1: merges read 128-bit windows of the longer list
+    int64_t pool = 1;           // 1: graph arrays and construction temporaries from a retained stream-ordered pool
     int64_t merge_alpha4[3] = {4, 4, 4};  // merge-vs-search weight x4 per length bucket
 };
 Options& options();
@@ -132,4 +133,6 @@ struct gpm_graph {
     int32_t* orig_col = nullptr;
     int device = 0;
     bool relabelled = false;
+    bool pooled = false;     // the arrays come from the device's stream-ordered pool
+    void* stream = nullptr;  // the stream their pooled frees are ordered on
 };

@@ -79,6 +79,9 @@ struct alignas(16) WarpState {
 // sees the loop exhausted, and only the owner frees a slot, after the last
 // slice has been taken (helpers keep their own copies of what they need).
 constexpr int kDonSlots = 1024;
+// list elements (candidate degrees) one loop slice covers at most, unless it
+// is a single candidate
+constexpr unsigned kLoopBudget = 16384;
 constexpr int kErrDonation = 4;
 
 // Record kinds: a loop of depth d, the batched deepest level (taken in
@@ -1338,12 +1341,31 @@ struct WarpCtx {
         __syncwarp();
     }
 
-    // Publishes the loop of depth d (just started) when it is long enough
-    // and a slot is free; the owner's own range then comes from claims.
+    // Publishes the loop of depth d (just started) when it is long enough —
+    // split_min candidates, or fewer whose neighbour lists hold at least
+    // kLoopBudget elements (a short loop over hubs: each iteration is a
+    // long intersection) — and a slot is free; the owner's own range then
+    // comes from claims.
     __device__ void maybe_donate(int d) {
         if (!don || split_min <= 0) return;
         const int e = s->end[d];
-        if (e < split_min || e > 0xffffff) return;
+        if (e < 2 || e > 0xffffff) return;
+        if (e < split_min) {
+            const int* list = s->lp[d];
+            unsigned long long work = 0;
+            for (int base = 0; base < e; base += 32) {
+                const int j = base + lane;
+                unsigned dg = 0;
+                if (j < e) {
+                    const int v = list[j];
+                    dg = g.rowptr[v + 1] - g.rowptr[v];
+                }
+#pragma unroll
+                for (int o = 16; o >= 1; o >>= 1) dg += __shfl_xor_sync(kFull, dg, o);
+                work += dg;
+            }
+            if (work < kLoopBudget) return;
+        }
         __syncwarp();
         if (lane == 0) {
             int h = -1;
@@ -1378,7 +1400,6 @@ struct WarpCtx {
     // descending degree, so the hubs at a loop's start come one per slice
     // instead of 64 to the first claimer.
     __device__ bool claim_more(int d) {
-        constexpr unsigned kLoopBudget = 16384;
         __syncwarp();
         if ((unsigned)s->dslot[d] >= (unsigned)kDonSlots) {
             if (lane == 0) record_check(kErrDonation, d, s->dslot[d], 0, 0, 0, 1);

@@ -300,9 +300,13 @@ GPM_API int gpm_count_noalloc(int32_t v_cnt, const uint32_t* d_rowptr, const int
  *   of at most 8 warps per SM),
  *   "stage_tma" (1: stage fixed leaf sets with bulk copies), "merge_vec"
  *   (1: merges read 128-bit windows), "schedule_gpu" (1: Schedule scores
- *   its candidates on the GPU when one is present),
- *   "split" (a loop at depth >= 2 with at least this many candidates is
- *   published so that idle warps take slices of it; 0 = off),
+ *   its candidates on the GPU when one is present), "pool" (1: graph
+ *   arrays and construction temporaries from a stream-ordered pool that
+ *   keeps freed memory, up to a quarter of the device, for the next upload),
+ *   "split" (a loop at depth >= 2 with at least this many candidates, or
+ *   fewer whose neighbour lists hold 16384 elements, is published so that
+ *   idle warps take slices of it, weighted by the candidates' degrees;
+ *   0 = off),
  *   "stage_max" (largest father set staged in shared memory),
  *   "leaf_batch", "pair_leaf" (batched deepest levels where the plan
  *   allows; the pair-sum leaf is on by default, the batched leaf off),

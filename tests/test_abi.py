@@ -118,7 +118,7 @@ def test_engine_defaults_and_option_checks(engine):
     # the shipped defaults (each chosen by measurement) and the range checks
     want = {"split": 64, "pair_leaf": 1, "leaf_batch": 0, "dense_slots": 64, "pair_max_ops": 0, "bitmap_min": 4096,
             "min_blocks": 1, "stripes": 1, "stripe": 0, "raw_sums": 0, "pair_log2": 0, "stage_tma": 1,
-            "merge_vec": 1, "schedule_gpu": 1}
+            "merge_vec": 1, "schedule_gpu": 1, "pool": 1}
     for k, v in want.items():
         assert gp.get_option(k) == v, k
     for bad in (("min_blocks", 2), ("split", -1), ("pair_log2", 25), ("stripes", 0), ("no_such_knob", 1)):
