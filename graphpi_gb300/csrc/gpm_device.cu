@@ -181,13 +181,72 @@ __global__ void __launch_bounds__(256) clique_kernel(GraphView g, int k, unsigne
     if (lane == 0 && acc != 0) add128(out, acc);
 }
 
-// CSR checks in one streaming pass: offsets monotone, ids in range, rows
-// strictly increasing, no self loops, and symmetry.  Symmetry is checked
-// without searching: the sums over all directed edges (u, v) of two 64-bit
-// mixes of the key (u, v) must equal the sums over the reversed keys
-// (v, u); an edge list that is not symmetric passes only if two
-// independent 64-bit sums collide (about 2^-128 for any fixed input).
-// words[0]: flag bits (atomicOr on its low word), words[1..4]: the sums.
+// Row of position k of a CSR: the last r in [0, V) with rowptr[r] <= k
+// (a binary search over the offsets; k < rowptr[V]).
+__device__ int csr_row_of(const unsigned* __restrict__ rowptr, int V, unsigned long long k) {
+    int lo = 0, hi = V - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((unsigned long long)rowptr[mid] <= k) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Rows of the 32 positions kb + lane (those below end): r0 is a row that
+// starts at or before kb.  Each round, lane j holds the start of row
+// r0 + 1 + j and every position finds how many of those starts it has
+// passed with a 5-step shuffle search; positions past all 32 move r0 on by
+// 32 rows and search again (rows of degree 0 are passed 32 at a time).
+// Returns this lane's row and leaves r0 at the batch's last row.
+__device__ int csr_batch_row(const unsigned* __restrict__ rowptr, int V, unsigned long long kb,
+                             unsigned long long end, int& r0, int lane) {
+    const unsigned long long k = kb + (unsigned long long)lane;
+    int row = r0;
+    bool done = k >= end;
+    int base = r0;
+    for (int round = 0; round < (1 << 26); ++round) {
+        if (__all_sync(kFull, done)) break;
+        const int r = base + 1 + lane;
+        const unsigned long long start = r < V ? (unsigned long long)rowptr[r] : ~0ull;
+        int c = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const unsigned long long sq = __shfl_sync(kFull, start, c + step - 1);
+            if (sq <= k) c += step;
+        }
+        const unsigned long long s31 = __shfl_sync(kFull, start, 31);
+        if (!done) {
+            if (c == 31 && s31 <= k) {
+                row = base + 32;  // at least: search on from there
+            } else {
+                row = base + c;
+                done = true;
+            }
+        }
+        base += 32;
+    }
+    // the batch's last row: the largest row of the lanes below end
+    int last = k < end ? row : -1;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) last = max(last, __shfl_xor_sync(kFull, last, o));
+    if (last >= 0) r0 = last;
+    return row;
+}
+
+// CSR checks in one streaming pass (the graph's own load-time checks): the
+// offsets are nondecreasing and end at e_cnt (each vertex, one thread);
+// then the edge positions in chunks of kValidateChunk per warp, each
+// position's row found by csr_batch_row: ids in range, no self loops,
+// lists strictly increasing, and symmetry — the sum over edges of a 64-bit
+// mix of (u, v) equals the sum of the mix of (v, u) exactly when every edge
+// has its reverse (as multisets; duplicates are already excluded), under
+// two salts so that a false match needs two independent 64-bit sums to
+// collide (about 2^-128 for any fixed input).  words[0]: flag bits
+// (atomicOr on its low word), words[1..4]: the sums.  The position pass
+// reads rows only through the offsets, which stay in [0, V) even when they
+// are malformed (flag 1 then reports it).
+constexpr unsigned kValidateChunk = 4096;
 __device__ __forceinline__ unsigned long long edge_mix(unsigned long long key, unsigned long long salt) {
     unsigned long long z = key + salt;
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -198,29 +257,44 @@ constexpr unsigned long long kSalt1 = 0x9E3779B97F4A7C15ull, kSalt2 = 0xD1B54A32
 
 __global__ void validate_kernel(GraphView g, unsigned long long* __restrict__ words) {
     const int lane = threadIdx.x & 31;
-    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long nthreads = (long long)gridDim.x * blockDim.x;
     unsigned bad = 0;
-    unsigned long long f1 = 0, b1 = 0, f2 = 0, b2 = 0;
-    for (long long v = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); v < g.v_cnt; v += warps) {
+    for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < g.v_cnt; v += nthreads) {
         const unsigned a = g.rowptr[v], b = g.rowptr[v + 1];
-        if (b < a || b > g.e_cnt) {
-            bad |= 1;
-            continue;
-        }
-        for (unsigned k = a + lane; k < b; k += 32) {
-            const int x = g.col[k];
-            if (x < 0 || x >= g.v_cnt) {
-                bad |= 2;
-                continue;
+        if (b < a || b > g.e_cnt) bad |= 1;
+    }
+    unsigned long long f1 = 0, b1 = 0, f2 = 0, b2 = 0;
+    const unsigned long long E = g.e_cnt;
+    const long long nw = nthreads >> 5;
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (unsigned long long c0 = (unsigned long long)w0 * kValidateChunk; c0 < E;
+         c0 += (unsigned long long)nw * kValidateChunk) {
+        const unsigned long long c1 = min(E, c0 + kValidateChunk);
+        int r0 = 0;
+        if (lane == 0) r0 = csr_row_of(g.rowptr, g.v_cnt, c0);
+        r0 = __shfl_sync(kFull, r0, 0);
+        for (unsigned long long kb = c0; kb < c1; kb += 32) {
+            const int row = csr_batch_row(g.rowptr, g.v_cnt, kb, c1, r0, lane);
+            const unsigned long long k = kb + (unsigned long long)lane;
+            const int x = k < c1 ? g.col[k] : 0;
+            const int left = __shfl_up_sync(kFull, x, 1);
+            if (k < c1) {
+                if (x < 0 || x >= g.v_cnt) {
+                    bad |= 2;
+                } else {
+                    if (x == row) bad |= 4;
+                    if (k > (unsigned long long)g.rowptr[row]) {
+                        const int prev = lane ? left : g.col[k - 1];
+                        if (prev >= x) bad |= 8;
+                    }
+                    const unsigned long long kf = ((unsigned long long)(unsigned)row << 32) | (unsigned)x;
+                    const unsigned long long kr = ((unsigned long long)(unsigned)x << 32) | (unsigned)row;
+                    f1 += edge_mix(kf, kSalt1);
+                    b1 += edge_mix(kr, kSalt1);
+                    f2 += edge_mix(kf, kSalt2);
+                    b2 += edge_mix(kr, kSalt2);
+                }
             }
-            if (x == (int)v) bad |= 4;
-            if (k > a && g.col[k - 1] >= x) bad |= 8;
-            const unsigned long long kf = ((unsigned long long)v << 32) | (unsigned)x;
-            const unsigned long long kb = ((unsigned long long)(unsigned)x << 32) | (unsigned long long)v;
-            f1 += edge_mix(kf, kSalt1);
-            b1 += edge_mix(kb, kSalt1);
-            f2 += edge_mix(kf, kSalt2);
-            b2 += edge_mix(kb, kSalt2);
         }
     }
 #pragma unroll
@@ -267,15 +341,33 @@ __global__ void relabel_maps_kernel(const unsigned* __restrict__ rowptr, const i
     }
 }
 
+// The relabelled edges in new-row order, unsorted within a row: output
+// position p of new row i (old vertex order[i]) takes the new id of the old
+// list's element at the same offset, and src[p] = i.  Positions go in
+// chunks per warp as in validate_kernel.
 __global__ void relabel_fill_kernel(const unsigned* __restrict__ rowptr, const int* __restrict__ col,
                                     const int* __restrict__ order, const int* __restrict__ new_id,
-                                    const unsigned* __restrict__ new_rowptr, int v_cnt, int* __restrict__ out) {
+                                    const unsigned* __restrict__ new_rowptr, int v_cnt, unsigned long long e_cnt,
+                                    unsigned* __restrict__ out, int* __restrict__ src) {
     const int lane = threadIdx.x & 31;
-    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long i = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < v_cnt; i += warps) {
-        const int o = order[i];
-        const unsigned a = rowptr[o], b = rowptr[o + 1], dst = new_rowptr[i];
-        for (unsigned k = a + lane; k < b; k += 32) out[dst + (k - a)] = new_id[col[k]];
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    for (unsigned long long c0 = (unsigned long long)w0 * kValidateChunk; c0 < e_cnt;
+         c0 += (unsigned long long)nw * kValidateChunk) {
+        const unsigned long long c1 = min(e_cnt, c0 + kValidateChunk);
+        int r0 = 0;
+        if (lane == 0) r0 = csr_row_of(new_rowptr, v_cnt, c0);
+        r0 = __shfl_sync(kFull, r0, 0);
+        for (unsigned long long pb = c0; pb < c1; pb += 32) {
+            const int i = csr_batch_row(new_rowptr, v_cnt, pb, c1, r0, lane);
+            const unsigned long long q = pb + (unsigned long long)lane;
+            if (q < c1) {
+                const int o = order[i];
+                const unsigned long long k = (unsigned long long)rowptr[o] + (q - new_rowptr[i]);
+                out[q] = (unsigned)new_id[col[k]];
+                src[q] = i;
+            }
+        }
     }
 }
 
@@ -451,12 +543,18 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     g->max_isect = V >= 2 ? (int)~top[1] : g->max_degree;
     if (!relabel || V == 0 || E == 0) return GPM_OK;
 
-    DevBuf new_id, new_deg, new_rowptr, new_col_u, new_col, tmp2;
+    // The relabelled lists come out sorted from one stable radix sort of the
+    // edges (new source i, new destination j) by j: the fill writes them in
+    // increasing i, and the graph is symmetric, so row j of the result lists
+    // its neighbours i in increasing order.
+    DevBuf new_id, new_deg, new_rowptr, keys_a, keys_b, vals_a, vals_b, tmp2;
     GPM_CK(new_id.alloc(c, sizeof(int) * (size_t)V));
     GPM_CK(new_deg.alloc(c, sizeof(unsigned) * ((size_t)V + 1)));
     GPM_CK(new_rowptr.alloc(c, sizeof(unsigned) * ((size_t)V + 1), g->pooled));
-    GPM_CK(new_col_u.alloc(c, sizeof(int) * (size_t)E));
-    GPM_CK(new_col.alloc(c, sizeof(int) * (size_t)E + kCsrSlack, g->pooled));
+    GPM_CK(keys_a.alloc(c, sizeof(unsigned) * (size_t)E));
+    GPM_CK(keys_b.alloc(c, sizeof(unsigned) * (size_t)E));
+    GPM_CK(vals_a.alloc(c, sizeof(int) * (size_t)E + kCsrSlack, g->pooled));
+    GPM_CK(vals_b.alloc(c, sizeof(int) * (size_t)E + kCsrSlack, g->pooled));
     relabel_maps_kernel<<<blocks, threads, 0, st>>>(g->rowptr, (const int*)order.p, V, (int*)new_id.p,
                                                     (unsigned*)new_deg.p);
     GPM_CK(cudaGetLastError());
@@ -465,15 +563,19 @@ static int relabel_graph(DeviceCtx* c, gpm_graph* g, bool relabel) {
     GPM_CK(tmp2.alloc(c, std::max<size_t>(sb, 1)));
     GPM_CK(cub::DeviceScan::ExclusiveSum(tmp2.p, sb, (unsigned*)new_deg.p, (unsigned*)new_rowptr.p, V + 1, st));
     relabel_fill_kernel<<<blocks, threads, 0, st>>>(g->rowptr, g->col, (const int*)order.p, (const int*)new_id.p,
-                                                    (const unsigned*)new_rowptr.p, V, (int*)new_col_u.p);
+                                                    (const unsigned*)new_rowptr.p, V, (unsigned long long)E,
+                                                    (unsigned*)keys_a.p, (int*)vals_a.p);
     GPM_CK(cudaGetLastError());
+    int end_bit = 1;
+    while (end_bit < 32 && (1ull << end_bit) < (unsigned long long)V) ++end_bit;
+    cub::DoubleBuffer<unsigned> dkeys((unsigned*)keys_a.p, (unsigned*)keys_b.p);
+    cub::DoubleBuffer<int> dvals((int*)vals_a.p, (int*)vals_b.p);
     size_t ssb = 0;
-    GPM_CK(cub::DeviceSegmentedSort::SortKeys(nullptr, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
-                                              (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
+    GPM_CK(cub::DeviceRadixSort::SortPairs(nullptr, ssb, dkeys, dvals, (unsigned long long)E, 0, end_bit, st));
     DevBuf tmp3;
     GPM_CK(tmp3.alloc(c, std::max<size_t>(ssb, 1)));
-    GPM_CK(cub::DeviceSegmentedSort::SortKeys(tmp3.p, ssb, (const int*)new_col_u.p, (int*)new_col.p, (int64_t)E, V,
-                                              (const unsigned*)new_rowptr.p, (const unsigned*)new_rowptr.p + 1, st));
+    GPM_CK(cub::DeviceRadixSort::SortPairs(tmp3.p, ssb, dkeys, dvals, (unsigned long long)E, 0, end_bit, st));
+    DevBuf& new_col = dvals.Current() == (int*)vals_a.p ? vals_a : vals_b;
     GPM_CK(cudaStreamSynchronize(st));
     // the caller's ids stay resident for label-sensitive plans
     g->orig_rowptr = g->rowptr;
