@@ -382,6 +382,11 @@ struct DeviceCtx {
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
     cudaMemPool_t pool = nullptr;  // graph arrays and construction temporaries (null: cudaMalloc)
+    // the dense counter arrays of the scratch known to be zero (every pair
+    // sum zeroes what it counted; a failed launch or another use of the
+    // scratch clears this, and the next launch zeroes the arrays again)
+    const void* dense_clean = nullptr;
+    size_t dense_clean_bytes = 0;
     std::mutex mu;
 };
 
@@ -452,6 +457,8 @@ static DeviceCtx* get_ctx(int* err) {
 
 static int ensure_scratch(DeviceCtx* c, size_t bytes) {
     if (c->scratch_bytes >= bytes) return GPM_OK;
+    c->dense_clean = nullptr;
+    c->dense_clean_bytes = 0;
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     c->scratch_bytes = 0;
@@ -825,8 +832,10 @@ static ScratchLayout scratch_layout(const LaunchSetup& ls) {
 
 static size_t scratch_bytes(const LaunchSetup& ls) { return scratch_layout(ls).total; }
 
+// zero_dense: zero the dense counter arrays first (they are new, or a failed
+// launch may have left counts in them)
 static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d_pairs,
-                                 unsigned long long* d_small, int* scratch, cudaStream_t st) {
+                                 unsigned long long* d_small, int* scratch, bool zero_dense, cudaStream_t st) {
     unsigned long long* cursors = d_small;
     unsigned long long* out = cursors + n;
     unsigned long long* stats = out + 2 * n;
@@ -844,7 +853,7 @@ static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d
         if (e != cudaSuccess) return e;
     }
     unsigned* dense = ls.dense_slots ? (unsigned*)((char*)scratch + lay.dense) : nullptr;
-    if (dense) {
+    if (dense && zero_dense) {
         const cudaError_t e = cudaMemsetAsync(dense, 0, dense_bytes(ls), st);
         if (e != cudaSuccess) return e;
     }
@@ -884,8 +893,14 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     init[3 * n + 3] = (unsigned long long)options().stripe;
     GPM_CK(cudaMemcpyAsync(d_pairs.p, ls.descs.data(), sizeof(PairDesc) * n, cudaMemcpyHostToDevice, st));
     GPM_CK(cudaMemcpyAsync(d_small.p, init.data(), words * sizeof(unsigned long long), cudaMemcpyHostToDevice, st));
+    const void* dense_ptr = ls.dense_slots ? (const char*)c->scratch + scratch_layout(ls).dense : nullptr;
+    const size_t dbytes = dense_bytes(ls);
+    const bool zero = dense_ptr && !(c->dense_clean == dense_ptr && c->dense_clean_bytes == dbytes);
+    c->dense_clean = nullptr;  // until this launch has finished cleanly
+    c->dense_clean_bytes = 0;
     GPM_CK(cudaEventRecord(c->ev0, st));
-    GPM_CK(enqueue_match(ls, n, (const PairDesc*)d_pairs.p, (unsigned long long*)d_small.p, (int*)c->scratch, st));
+    GPM_CK(enqueue_match(ls, n, (const PairDesc*)d_pairs.p, (unsigned long long*)d_small.p, (int*)c->scratch, zero,
+                         st));
     GPM_CK(cudaEventRecord(c->ev1, st));
     std::vector<unsigned long long> raw(2 * n + 2);
     GPM_CK(cudaMemcpyAsync(raw.data(), (unsigned long long*)d_small.p + n, sizeof(unsigned long long) * (2 * n + 2),
@@ -897,7 +912,12 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     t_launches = 1;
     t_bytes = raw[2 * n];
     memcpy(host_raw, raw.data(), sizeof(unsigned long long) * 2 * n);
-    return take_check("pattern matching");
+    rc = take_check("pattern matching");
+    if (rc == GPM_OK && dense_ptr) {
+        c->dense_clean = dense_ptr;
+        c->dense_clean_bytes = dbytes;
+    }
+    return rc;
 }
 
 static int finish_counts(int n, const gpm_plan* const* plans, const unsigned long long* raw, gpm_u128* outs) {
@@ -1239,6 +1259,8 @@ GPM_API int gpm_clique_count(gpm_graph* g, int32_t k, gpm_u128* out) {
     const size_t per_warp = (size_t)std::max(1, k - 3) * (size_t)std::max(1, g->max_degree);
     int rc = ensure_scratch(c, warps * per_warp * sizeof(int));
     if (rc) return rc;
+    c->dense_clean = nullptr;  // the clique kernel writes over the matcher's scratch
+    c->dense_clean_bytes = 0;
     DevBuf buf;
     // cursor, 128-bit count, stripes, stripe
     GPM_CK(buf.alloc(c, 5 * sizeof(unsigned long long)));
@@ -1360,6 +1382,7 @@ struct gpm_batch_exec {
     unsigned long long* d_small = nullptr;
     unsigned long long* h_small = nullptr;  // pinned: out[2n], stats[2], params[2]
     int* scratch = nullptr;
+    bool dense_dirty = true;  // zero the dense counter arrays before the next replay
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     ~gpm_batch_exec() {
@@ -1392,7 +1415,7 @@ static int exec_build(DeviceCtx* c, gpm_batch_exec* e, gpm_graph* const* graphs)
     GPM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaMemcpyAsync(d_params, h_params, 2 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(e->d_small, 0, (3 * (size_t)n + 2) * sizeof(unsigned long long), st);
-    const cudaError_t qe = enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, st);
+    const cudaError_t qe = enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, false, st);
     cudaMemcpyAsync(e->h_small, e->d_small + n, (2 * (size_t)n + 2) * sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, st);
     cudaGraph_t g = nullptr;
@@ -1440,6 +1463,11 @@ GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph
     e->h_small[2 * n + 2] = (unsigned long long)options().stripes;
     e->h_small[2 * n + 3] = (unsigned long long)options().stripe;
     cudaStream_t st = c->stream;
+    if (e->dense_dirty && e->ls.dense_slots) {
+        // the replayed launch leaves them zero; zeroed here when new or after a failure
+        GPM_CK(cudaMemsetAsync((char*)e->scratch + scratch_layout(e->ls).dense, 0, dense_bytes(e->ls), st));
+    }
+    e->dense_dirty = true;
     GPM_CK(cudaEventRecord(c->ev0, st));
     GPM_CK(cudaGraphLaunch(e->exec, st));
     GPM_CK(cudaEventRecord(c->ev1, st));
@@ -1452,6 +1480,7 @@ GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph
     std::vector<unsigned long long> raw(e->h_small, e->h_small + 2 * n);
     int rc = take_check("gpm_batch_exec_run");
     if (rc) return rc;
+    e->dense_dirty = false;
     return finish_counts(n, e->plans.data(), raw.data(), outs);
 }
 

@@ -135,46 +135,88 @@ static_assert(sizeof(Donation) == 64, "one record per 64 bytes");
 
 struct DonationArea {
     Donation rec[kDonSlots];
-    unsigned busy[kDonSlots];  // 1 while a record's owner holds the slot
-    unsigned finished;         // warps done with their own queues
-    unsigned held;             // slots held by owners (records that may be live)
+    unsigned busy[kDonSlots];    // 1 while a record's owner holds the slot
+    unsigned visits[kDonSlots];  // helpers that may still claim from a record
+    unsigned finished;           // warps done with their own queues
+    unsigned held;               // slots held by owners (records that may be live)
     unsigned pad_[2];
 };
+
+// Claims are fetch-and-adds on the record word's next field, so that any
+// number of warps can take slices of one record at once (a compare-and-swap
+// per claim let one claim through per round trip while every other warp
+// retried).  An add cannot check the generation first, so a warp registers
+// as a visitor of the record (visits[h]) before it reads the word and stays
+// one until it stops claiming; an owner publishes a new generation in a
+// record only when it has no visitors: a slot is taken only if unvisited,
+// and a pair sum waits for its helpers to leave between phases.  So every
+// add lands in the generation its warp checked.  The next field may run
+// past end by one slice per claimer; end stays below kDonEndMax so that it
+// never carries into end.
+constexpr unsigned kDonEndMax = 0xf00000u;
 
 __device__ __forceinline__ unsigned long long don_pack(unsigned gen, unsigned end, unsigned next) {
     return ((unsigned long long)(gen & 0xffffu) << 48) | ((unsigned long long)(end & 0xffffffu) << 24) |
            (unsigned long long)(next & 0xffffffu);
 }
 
-// Takes the next slice of record r (generation gen); lo == hi when the loop
-// is exhausted or the slot holds another generation.  A slice is 1/32 of
-// what is left, within the bounds of the record's kind.  Lock-free: a failed compare-and-swap means another
-// warp took a slice, so the retries are bounded by the loop length (< 2^24).
+// Adds take to record r's next field (the caller visits r and has seen
+// generation gen in it); returns the slice [lo, hi), empty when the record
+// was exhausted.
+__device__ void don_take(Donation* r, unsigned gen, unsigned take, int& lo, int& hi) {
+    lo = hi = 0;
+    const unsigned long long old = atomicAdd(&r->word, (unsigned long long)take);
+    const unsigned end = (unsigned)(old >> 24) & 0xffffffu, next = (unsigned)old & 0xffffffu;
+    if ((unsigned)(old >> 48) != (gen & 0xffffu) || next + take > 0xffffffu) {
+        record_check(kErrDonation, gen, (long long)old, take, 0, 0, 5);
+        return;
+    }
+    if (next >= end) return;
+    lo = (int)next;
+    hi = (int)min(next + take, end);
+}
+
+// Takes the next slice of record r (generation gen, visited by the caller);
+// lo == hi when the record is exhausted or holds another generation.  A
+// slice is 1/32 of what is left, within the bounds of the record's kind: a
+// loop's first slice for a helper one candidate (its later slices are
+// weighted by claim_more), batched leaves [8, 128], pair-sum lengths [1, 16]
+// blocks of 32 candidates, pair-sum element phases [1, 64] units (of 64
+// elements or more).
 __device__ void don_claim(Donation* r, unsigned gen, int kind, int& lo, int& hi) {
     lo = hi = 0;
-    unsigned long long w = *(volatile unsigned long long*)&r->word;
-    // slice bounds per kind: a loop's first slice for a helper one candidate
-    // (its later slices are weighted by claim_more), batched leaves [8, 128],
-    // pair-sum lengths [1, 16] blocks of 32 candidates, pair-sum element
-    // phases [1, 64] units (of 64 elements or more)
+    const unsigned long long w = *(volatile unsigned long long*)&r->word;
+    if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
+    const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
+    if (next >= end) return;
     kind &= 0xff;
     const unsigned smin = kind == kDonLeaf ? 8u : 1u;
     const unsigned smax = kind == kDonLeaf ? 128u : (kind == kDonLoop ? 1u : (kind == kDonPairLen ? 16u : 64u));
-    for (int tries = 0; tries < (1 << 25); ++tries) {
-        if ((unsigned)(w >> 48) != (gen & 0xffffu)) return;
-        const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
-        if (next >= end) return;
-        const unsigned want = (end - next) >> 5;
-        const unsigned take = min(end - next, min(smax, max(smin, want)));
-        const unsigned long long got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
-        if (got == w) {
-            lo = (int)next;
-            hi = (int)(next + take);
-            return;
-        }
-        w = got;
+    const unsigned take = min(end - next, min(smax, max(smin, (end - next) >> 5)));
+    don_take(r, gen, take, lo, hi);
+}
+
+// A free, unvisited slot (lane 0): busy is taken, then the slot is given up
+// again if some warp may still claim from its last record.
+__device__ int don_take_slot(DonationArea* don, long long seed) {
+    for (int probe = 0; probe < 4; ++probe) {
+        const int c = (int)((seed + probe * 257) & (kDonSlots - 1));
+        if (atomicCAS(&don->busy[c], 0u, 1u) != 0u) continue;
+        __threadfence();
+        if (atomicAdd(&don->visits[c], 0u) == 0u) return c;
+        atomicExch(&don->busy[c], 0u);
     }
-    record_check(kErrDonation, gen, (long long)w, 0, 0, 0, 0);
+    return -1;
+}
+
+// A helper's visit of record h: registered before it reads the record
+__device__ __forceinline__ void don_visit(DonationArea* don, int h) {
+    atomicAdd(&don->visits[h], 1u);
+    __threadfence();
+}
+__device__ __forceinline__ void don_leave(DonationArea* don, int h) {
+    __threadfence();
+    atomicAdd(&don->visits[h], ~0u);  // minus one
 }
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -887,13 +929,23 @@ struct WarpCtx {
     __device__ int take_slot(int salt) {
         int h = -1;
         if (lane == 0) {
-            for (int probe = 0; probe < 4 && h < 0; ++probe) {
-                const int c = (int)((gw * 7 + salt * 131 + probe * 257) & (kDonSlots - 1));
-                if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
-            }
+            h = don_take_slot(don, gw * 7 + salt * 131);
             if (h >= 0) atomicAdd(&don->held, 1u);
         }
         return __shfl_sync(kFull, h, 0);
+    }
+
+    // Before this owner publishes another phase in record h: every helper of
+    // the last phase has left (they leave once it is exhausted); bounded.
+    __device__ void pair_vacate(int h) {
+        unsigned v = 0;
+        for (int it = 0; it < (1 << 24); ++it) {
+            if (lane == 0) v = atomicAdd(&don->visits[h], 0u);
+            v = __shfl_sync(kFull, v, 0);
+            if (v == 0) return;
+            __nanosleep(128);
+        }
+        if (lane == 0) record_check(kErrDonation, h, v, 0, 0, 0, 6);
     }
 
     __device__ void drop_slot(int h) {
@@ -911,6 +963,7 @@ struct WarpCtx {
     // warp alone when h < 0.
     __device__ long long pair_phase(const PairCtx& c, int h, int kind, int units, unsigned tag, int aux) {
         if (h < 0) return pair_run(c, kind, 0, units);
+        pair_vacate(h);
         const unsigned gen = pair_publish(h, kind, units, tag, aux);
         const long long sum = pair_slices(h, gen, kind, c);
         pair_wait(h, units);
@@ -937,7 +990,7 @@ struct WarpCtx {
         out = 0;
         if (c.na == 0 || c.nb == 0) return true;
         const int nba = (c.na + 31) >> 5, nbb = (c.nb + 31) >> 5;
-        const bool can_share = don && split_min > 0 && nba + nbb <= 0xffffff;
+        const bool can_share = don && split_min > 0 && nba + nbb <= (int)kDonEndMax;
         int h = (can_share && nba + nbb >= kShareBlocks) ? take_slot(L1) : -1;
         pair_phase(c, h, kDonPairLen, nba + nbb, 0u, c.na);
         const unsigned ma = pair_scan(c.bsA, nba), mb = pair_scan(c.bsB, nbb);
@@ -992,7 +1045,7 @@ struct WarpCtx {
         // element units: 2^GPM_PAIR_UNIT_LOG2 elements, coarser when a side
         // would exceed 2^24 units
         int ul = GPM_PAIR_UNIT_LOG2;
-        while (((unsigned long long)maxs >> ul) >= 0xffffffull) ++ul;
+        while (((unsigned long long)maxs >> ul) >= (unsigned long long)kDonEndMax) ++ul;
         const unsigned long long um = (1ull << ul) - 1;
         const int ufill = (int)((mins + um) >> ul), uprobe = (int)((maxs + um) >> ul);
         const int fside = a_fills ? kDonSideA : 0, pside = a_fills ? 0 : kDonSideA;
@@ -1349,7 +1402,7 @@ struct WarpCtx {
     __device__ void maybe_donate(int d) {
         if (!don || split_min <= 0) return;
         const int e = s->end[d];
-        if (e < 2 || e > 0xffffff) return;
+        if (e < 2 || e > (int)kDonEndMax) return;
         if (e < split_min) {
             const int* list = s->lp[d];
             unsigned long long work = 0;
@@ -1368,11 +1421,7 @@ struct WarpCtx {
         }
         __syncwarp();
         if (lane == 0) {
-            int h = -1;
-            for (int probe = 0; probe < 4 && h < 0; ++probe) {
-                const int c = (int)((gw * 7 + d * 131 + probe * 257) & (kDonSlots - 1));
-                if (atomicCAS(&don->busy[c], 0u, 1u) == 0u) h = c;
-            }
+            const int h = don_take_slot(don, gw * 7 + d * 131);
             if (h >= 0) {
                 atomicAdd(&don->held, 1u);
                 Donation* r = &don->rec[h];
@@ -1410,15 +1459,16 @@ struct WarpCtx {
         const bool leaf = d == P->L && batch_on();
         const int* list = s->lp[d];
         int lo = 0, hi = 0;
-        for (int tries = 0; tries < (1 << 24); ++tries) {
-            unsigned long long w = 0;
-            if (lane == 0) w = *(volatile unsigned long long*)&r->word;
-            w = __shfl_sync(kFull, w, 0);
-            const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
-            if ((unsigned)(w >> 48) != gen || next >= end) break;
+        unsigned long long w = 0;
+        if (lane == 0) w = *(volatile unsigned long long*)&r->word;
+        w = __shfl_sync(kFull, w, 0);
+        const unsigned end = (unsigned)(w >> 24) & 0xffffffu, next = (unsigned)w & 0xffffffu;
+        if ((unsigned)(w >> 48) == gen && next < end) {
             const unsigned smin = leaf ? 8u : 1u, smax = leaf ? 128u : 64u;
             unsigned take = min(end - next, min(smax, max(smin, (end - next) >> 5)));
             if (!leaf) {
+                // weighted from the candidates at the snapshot's next: the
+                // add may land further on, where degrees are no larger
                 const unsigned look = min(take, 32u);
                 unsigned dg = 0;
                 if ((unsigned)lane < look) {
@@ -1434,14 +1484,9 @@ struct WarpCtx {
                 const unsigned fit = __popc(__ballot_sync(kFull, (unsigned)lane < look && incl <= kLoopBudget));
                 if (fit < look) take = max(1u, fit);
             }
-            unsigned long long got = 0;
-            if (lane == 0) got = atomicCAS(&r->word, w, don_pack(gen, end, next + take));
-            got = __shfl_sync(kFull, got, 0);
-            if (got == w) {
-                lo = (int)next;
-                hi = (int)(next + take);
-                break;
-            }
+            if (lane == 0) don_take(r, gen, take, lo, hi);
+            lo = __shfl_sync(kFull, lo, 0);
+            hi = __shfl_sync(kFull, hi, 0);
         }
         __syncwarp();
         if (lane == 0 && hi > lo) {
@@ -1452,14 +1497,19 @@ struct WarpCtx {
         return hi > lo;
     }
 
-    // the donated loop at depth d is exhausted: its owner frees the slot
+    // the donated loop at depth d is exhausted: its owner frees the slot, a
+    // helper ends its visit
     __device__ void release(int d) {
         __syncwarp();
         if (lane == 0) {
-            if (s->downer[d] && (unsigned)s->dslot[d] < (unsigned)kDonSlots) {
-                __threadfence();
-                atomicExch(&don->busy[s->dslot[d]], 0u);
-                atomicAdd(&don->held, ~0u);  // minus one
+            if ((unsigned)s->dslot[d] < (unsigned)kDonSlots) {
+                if (s->downer[d]) {
+                    __threadfence();
+                    atomicExch(&don->busy[s->dslot[d]], 0u);
+                    atomicAdd(&don->held, ~0u);  // minus one
+                } else {
+                    don_leave(don, s->dslot[d]);
+                }
             }
             s->dslot[d] = -1;
         }
@@ -1570,6 +1620,9 @@ struct WarpCtx {
         int lo = 0, hi = 0, p = 0, d = 0, rend = 0, kind = 0, owner_w = 0, aux = 0;
         unsigned ep = 0;
         if (lane == 0) {
+            // a visitor from here on: no new generation is published in r
+            // until it leaves, so the fields read below stay the record's
+            don_visit(don, h);
             const unsigned long long w = *(volatile unsigned long long*)&r->word;
             if ((unsigned)(w >> 48) == gen && (w & 0xffffffu) < ((w >> 24) & 0xffffffu)) {
                 __threadfence();
@@ -1582,9 +1635,9 @@ struct WarpCtx {
                 ep = vr->epoch;
                 aux = vr->chosen[kMaxN - 1];
                 rend = (int)((w >> 24) & 0xffffffu);
-                // the claim succeeds only while the record still holds these fields
                 don_claim(r, gen, kind, lo, hi);
             }
+            if (hi <= lo) don_leave(don, h);
         }
         lo = __shfl_sync(kFull, lo, 0);
         hi = __shfl_sync(kFull, hi, 0);
@@ -1606,7 +1659,10 @@ struct WarpCtx {
             pair_kind && ((unsigned)owner_w >= gridDim.x * (blockDim.x >> 5) ||
                           (dense_kind ? (!dense || ep >= (unsigned)dense_slots) : (!len_kind && !ptab_base)));
         if (p < 0 || p >= npairs || bad_owner) {
-            if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
+            if (lane == 0) {
+                record_check(kErrDonation, h, p, d, lo, hi, rend);
+                don_leave(don, h);
+            }
             __syncwarp();
             return true;
         }
@@ -1634,14 +1690,20 @@ struct WarpCtx {
         }
         if (!ok) {
             // the rebuilt loop differs from the published one: the slice is lost
-            if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, rend);
+            if (lane == 0) {
+                record_check(kErrDonation, h, p, d, lo, hi, rend);
+                don_leave(don, h);
+            }
             __syncwarp();
             return true;
         }
         if (pair_kind) {
             if (dense_kind) {
                 if (g.v_cnt > dense_words) {
-                    if (lane == 0) record_check(kErrDonation, h, p, d, lo, hi, -3);
+                    if (lane == 0) {
+                        record_check(kErrDonation, h, p, d, lo, hi, -3);
+                        don_leave(don, h);
+                    }
                     __syncwarp();
                     return true;
                 }
@@ -1657,6 +1719,8 @@ struct WarpCtx {
                 atomicAdd(&r->done, (unsigned)(hi - lo));
             }
             sum += pair_slices(h, gen, kind, pc);
+            __syncwarp();
+            if (lane == 0) don_leave(don, h);  // the phase is exhausted
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(kFull, sum, o);
             if (lane == 0 && sum != 0) add128(out + 2 * p, (__int128)sum);
@@ -1672,6 +1736,7 @@ struct WarpCtx {
         }
         __syncwarp();
         const __int128 acc = (d == P->L && batch_on()) ? leaf_slices() : dfs_levels(d);
+        if (s->dslot[d] >= 0) release(d);  // left early (an internal check): end the visit
         if (lane == 0 && acc != 0) add128(out + 2 * p, acc);
         return true;
     }

@@ -188,6 +188,19 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
         }
     }
     for (auto& x : th) x.join();
+    if (don) {
+        // every visit ended and every slot given back
+        for (int h = 0; h < kDonSlots; ++h)
+            if (don->visits[h] || don->busy[h]) {
+                std::printf("donation slot %d left with %u visits, busy %u\n", h, don->visits[h], don->busy[h]);
+                ++failures;
+                break;
+            }
+        if (don->held) {
+            std::printf("donation slots still counted as held: %u\n", don->held);
+            ++failures;
+        }
+    }
     delete don;
     for (int w = 0; w < warps; ++w) {
         int* base = scratch.data() + (size_t)w * per_warp;

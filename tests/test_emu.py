@@ -8,7 +8,9 @@ its dense counter arrays (every phase shared, in one-element slices), leaf
 bitmaps, stripes that do not depend on the
 grab size and that add up to the whole job (the multi-rank split); any
 out-of-bounds access, any lane that meets a different shuffle/ballot/syncwarp
-than its warp, and any internal check stops the run."""
+than its warp, and any internal check stops the run.  After every launch the
+dense counters and leaf bitmaps must be zero again and every donation slot
+released with no visitor left (the claim protocol's bookkeeping)."""
 import os
 import shutil
 import subprocess
