@@ -387,6 +387,8 @@ struct DeviceCtx {
     // scratch clears this, and the next launch zeroes the arrays again)
     const void* dense_clean = nullptr;
     size_t dense_clean_bytes = 0;
+    const void* tables_clean = nullptr;  // likewise the pair-sum tables and their stored tags
+    size_t tables_clean_bytes = 0;
     std::mutex mu;
 };
 
@@ -459,6 +461,8 @@ static int ensure_scratch(DeviceCtx* c, size_t bytes) {
     if (c->scratch_bytes >= bytes) return GPM_OK;
     c->dense_clean = nullptr;
     c->dense_clean_bytes = 0;
+    c->tables_clean = nullptr;
+    c->tables_clean_bytes = 0;
     if (c->scratch) cudaFree(c->scratch);
     c->scratch = nullptr;
     c->scratch_bytes = 0;
@@ -811,13 +815,20 @@ static size_t bitmap_bytes(const LaunchSetup& ls) {
     return (size_t)ls.blocks * ls.wpb * 2 * (size_t)ls.bm_words * sizeof(unsigned);
 }
 
+// the warps' pair-sum tables, then one stored tag per warp (kept across
+// launches: zeroed only when new or after a failed launch)
+static size_t pair_region_bytes(const LaunchSetup& ls) {
+    const size_t warps = (size_t)ls.blocks * ls.wpb;
+    return warps * ((size_t)1 << ls.pair_log2) * sizeof(unsigned long long) + ((warps * sizeof(unsigned) + 255) & ~(size_t)255);
+}
+
 static ScratchLayout scratch_layout(const LaunchSetup& ls) {
     const size_t warps = (size_t)ls.blocks * ls.wpb;
     ScratchLayout s;
     size_t b = warps * (size_t)ls.per_warp * sizeof(int);
     b = (b + 255) & ~(size_t)255;
     s.tables = b;
-    if (ls.pair_on) b += warps * ((size_t)1 << ls.pair_log2) * sizeof(unsigned long long);
+    if (ls.pair_on) b += pair_region_bytes(ls);
     s.donation = b;
     if (ls.split_min > 0) b += sizeof(DonationArea);
     b = (b + 255) & ~(size_t)255;
@@ -832,16 +843,22 @@ static ScratchLayout scratch_layout(const LaunchSetup& ls) {
 
 static size_t scratch_bytes(const LaunchSetup& ls) { return scratch_layout(ls).total; }
 
-// zero_dense: zero the dense counter arrays first (they are new, or a failed
-// launch may have left counts in them)
+// zero_dense / zero_tables: zero the dense counter arrays / the pair-sum
+// tables and tags first (they are new, or a failed launch may have left
+// counts in them)
 static cudaError_t enqueue_match(const LaunchSetup& ls, int n, const PairDesc* d_pairs,
-                                 unsigned long long* d_small, int* scratch, bool zero_dense, cudaStream_t st) {
+                                 unsigned long long* d_small, int* scratch, bool zero_dense, bool zero_tables,
+                                 cudaStream_t st) {
     unsigned long long* cursors = d_small;
     unsigned long long* out = cursors + n;
     unsigned long long* stats = out + 2 * n;
     const unsigned long long* params = stats + 2;
     const ScratchLayout lay = scratch_layout(ls);
     unsigned long long* tables = ls.pair_on ? (unsigned long long*)((char*)scratch + lay.tables) : nullptr;
+    if (tables && zero_tables) {
+        const cudaError_t e = cudaMemsetAsync(tables, 0, pair_region_bytes(ls), st);
+        if (e != cudaSuccess) return e;
+    }
     DonationArea* don = ls.split_min > 0 ? (DonationArea*)((char*)scratch + lay.donation) : nullptr;
     if (don) {
         const cudaError_t e = cudaMemsetAsync(don, 0, sizeof(DonationArea), st);
@@ -896,11 +913,16 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     const void* dense_ptr = ls.dense_slots ? (const char*)c->scratch + scratch_layout(ls).dense : nullptr;
     const size_t dbytes = dense_bytes(ls);
     const bool zero = dense_ptr && !(c->dense_clean == dense_ptr && c->dense_clean_bytes == dbytes);
+    const void* tab_ptr = ls.pair_on ? (const char*)c->scratch + scratch_layout(ls).tables : nullptr;
+    const size_t tbytes = ls.pair_on ? pair_region_bytes(ls) : 0;
+    const bool zero_tab = tab_ptr && !(c->tables_clean == tab_ptr && c->tables_clean_bytes == tbytes);
     c->dense_clean = nullptr;  // until this launch has finished cleanly
     c->dense_clean_bytes = 0;
+    c->tables_clean = nullptr;
+    c->tables_clean_bytes = 0;
     GPM_CK(cudaEventRecord(c->ev0, st));
     GPM_CK(enqueue_match(ls, n, (const PairDesc*)d_pairs.p, (unsigned long long*)d_small.p, (int*)c->scratch, zero,
-                         st));
+                         zero_tab, st));
     GPM_CK(cudaEventRecord(c->ev1, st));
     std::vector<unsigned long long> raw(2 * n + 2);
     GPM_CK(cudaMemcpyAsync(raw.data(), (unsigned long long*)d_small.p + n, sizeof(unsigned long long) * (2 * n + 2),
@@ -913,9 +935,11 @@ static int run_pairs(DeviceCtx* c, int n, gpm_graph* const* graphs, const gpm_pl
     t_bytes = raw[2 * n];
     memcpy(host_raw, raw.data(), sizeof(unsigned long long) * 2 * n);
     rc = take_check("pattern matching");
-    if (rc == GPM_OK && dense_ptr) {
+    if (rc == GPM_OK) {
         c->dense_clean = dense_ptr;
-        c->dense_clean_bytes = dbytes;
+        c->dense_clean_bytes = dense_ptr ? dbytes : 0;
+        c->tables_clean = tab_ptr;
+        c->tables_clean_bytes = tbytes;
     }
     return rc;
 }
@@ -1261,6 +1285,8 @@ GPM_API int gpm_clique_count(gpm_graph* g, int32_t k, gpm_u128* out) {
     if (rc) return rc;
     c->dense_clean = nullptr;  // the clique kernel writes over the matcher's scratch
     c->dense_clean_bytes = 0;
+    c->tables_clean = nullptr;
+    c->tables_clean_bytes = 0;
     DevBuf buf;
     // cursor, 128-bit count, stripes, stripe
     GPM_CK(buf.alloc(c, 5 * sizeof(unsigned long long)));
@@ -1382,7 +1408,7 @@ struct gpm_batch_exec {
     unsigned long long* d_small = nullptr;
     unsigned long long* h_small = nullptr;  // pinned: out[2n], stats[2], params[2]
     int* scratch = nullptr;
-    bool dense_dirty = true;  // zero the dense counter arrays before the next replay
+    bool dense_dirty = true;  // zero the dense counter arrays and pair-sum tables before the next replay
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     ~gpm_batch_exec() {
@@ -1415,7 +1441,8 @@ static int exec_build(DeviceCtx* c, gpm_batch_exec* e, gpm_graph* const* graphs)
     GPM_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     cudaMemcpyAsync(d_params, h_params, 2 * sizeof(unsigned long long), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(e->d_small, 0, (3 * (size_t)n + 2) * sizeof(unsigned long long), st);
-    const cudaError_t qe = enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, false, st);
+    const cudaError_t qe =
+        enqueue_match(e->ls, n, (const PairDesc*)e->d_pairs, e->d_small, e->scratch, false, false, st);
     cudaMemcpyAsync(e->h_small, e->d_small + n, (2 * (size_t)n + 2) * sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, st);
     cudaGraph_t g = nullptr;
@@ -1463,9 +1490,13 @@ GPM_API int gpm_batch_exec_run(gpm_batch_exec** exec, int32_t n_pairs, gpm_graph
     e->h_small[2 * n + 2] = (unsigned long long)options().stripes;
     e->h_small[2 * n + 3] = (unsigned long long)options().stripe;
     cudaStream_t st = c->stream;
-    if (e->dense_dirty && e->ls.dense_slots) {
-        // the replayed launch leaves them zero; zeroed here when new or after a failure
-        GPM_CK(cudaMemsetAsync((char*)e->scratch + scratch_layout(e->ls).dense, 0, dense_bytes(e->ls), st));
+    if (e->dense_dirty) {
+        // the replayed launch leaves the counters zero and the tables' tags
+        // current; zeroed here when new or after a failure
+        if (e->ls.dense_slots)
+            GPM_CK(cudaMemsetAsync((char*)e->scratch + scratch_layout(e->ls).dense, 0, dense_bytes(e->ls), st));
+        if (e->ls.pair_on)
+            GPM_CK(cudaMemsetAsync((char*)e->scratch + scratch_layout(e->ls).tables, 0, pair_region_bytes(e->ls), st));
     }
     e->dense_dirty = true;
     GPM_CK(cudaEventRecord(c->ev0, st));

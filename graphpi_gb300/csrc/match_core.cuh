@@ -1854,7 +1854,17 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : (kMinBlocks == 5 ? 128
     w.ptab = pair_tables ? pair_tables + ((size_t)gw << pair_log2) : nullptr;
     w.ptab_base = pair_tables;
     w.pair_log2 = pair_log2;
-    if (lane == 0) w.s->epoch = 0;  // the first pair sum clears the table
+    // Each warp's table keeps its entries across launches: the warp's last
+    // tag is stored after all tables (one word per warp), so a table is
+    // cleared only when its cycle of tags wraps, not in every launch.  A
+    // stored 0 (tables just zeroed by the host) reads as 1, a tag no entry
+    // of a zeroed table carries.
+    unsigned* const pair_epochs =
+        pair_tables ? reinterpret_cast<unsigned*>(pair_tables + (((size_t)gridDim.x * nwarps) << pair_log2)) : nullptr;
+    if (lane == 0) {
+        const unsigned e = pair_epochs ? pair_epochs[gw] : 0u;
+        w.s->epoch = e ? e : 1u;
+    }
     w.scratch = scratch_all + gw * scratch_per_warp;
     w.spw = scratch_per_warp;
     w.lane = lane;
@@ -1927,4 +1937,5 @@ __global__ void __launch_bounds__(kMinBlocks == 1 ? 512 : (kMinBlocks == 5 ? 128
         w.help_all(pairs, npairs, out, gridDim.x * (unsigned)nwarps);
     }
     if (kBytes && lane == 0 && w.bytes) atomicAdd(stats, w.bytes);
+    if (lane == 0 && pair_epochs) pair_epochs[gw] = w.s->epoch;
 }

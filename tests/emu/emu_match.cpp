@@ -113,6 +113,9 @@ struct Knobs {
     int bm_min = 0;  // > 0: leaf bitmaps for fixed sets of at least this size
     int dense = 0;   // > 0: that many dense counter arrays for big pair sums
     unsigned long long stripes = 1, stripe = 0;
+    // pair-sum tables kept across launches (their stored tags too), as the
+    // engine keeps them; null: fresh zeroed tables for this launch
+    std::vector<unsigned long long>* keep_tables = nullptr;
 };
 
 // One emulated launch over all pairs; returns the raw 128-bit sums.
@@ -146,7 +149,11 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
     std::vector<unsigned long long> cursors(n, 0), out(2 * n, 0), stats(2, 0);
     unsigned long long params[2] = {k.stripes, k.stripe};
     std::vector<unsigned long long> tables;
-    if (k.pair) tables.assign((size_t)warps << k.pair_log2, 0ull);
+    // the tables, then one stored tag per warp (zero: fresh tables)
+    const size_t table_words = ((size_t)warps << k.pair_log2) + (size_t)warps;
+    if (k.pair && k.keep_tables && k.keep_tables->size() != table_words) k.keep_tables->assign(table_words, 0ull);
+    if (k.pair && !k.keep_tables) tables.assign(table_words, 0ull);
+    unsigned long long* tab = !k.pair ? nullptr : (k.keep_tables ? k.keep_tables->data() : tables.data());
     const int bm_words = k.bm_min > 0 ? (g.v + 31) / 32 : 0;
     // dense pool: lock words padded to 64, then k.dense arrays of g.v counters
     std::vector<unsigned> dense(k.dense ? 64 + (size_t)k.dense * g.v : 0, 0u);
@@ -170,7 +177,7 @@ std::vector<__int128> launch(const Csr& g, const std::vector<Sched>& ss, const K
                 }
                 auto body = [&](int) {
                     match_kernel<false, 1>(pairs.data(), n, cursors.data(), out.data(), scratch.data(), per_warp, k.chunk,
-                                        params, k.leaf, k.stage_cap, k.pair, k.pair ? tables.data() : nullptr, k.pair_log2, don,
+                                        params, k.leaf, k.stage_cap, k.pair, tab, k.pair_log2, don,
                                         k.split, bm_words ? bitmaps.data() : nullptr, bm_words, k.bm_min,
                                         k.dense ? dense.data() : nullptr, k.dense, g.v, stats.data());
                 };
@@ -374,6 +381,25 @@ void case_pairhub() {
     }
 }
 
+// pair-sum tables kept across launches: entries of earlier launches carry
+// older tags and are never read as live
+void case_pairtags() {
+    const Csr g = chung_lu(600, 8.0, 2.1, 250, 14);
+    std::vector<Sched> ss;
+    for (const Sched& s : motif_schedules(g, 5, true, 1))
+        if (s.plan.pair_ok) ss.push_back(s);
+    std::vector<unsigned long long> keep;
+    for (int rep = 0; rep < 3; ++rep) {
+        Knobs k;
+        k.pair = 1;
+        k.split = rep == 1 ? 0 : 1;
+        k.pair_log2 = 13;
+        k.dense = 2;
+        k.keep_tables = &keep;
+        expect_oracle("pair-sum, tables kept across launches", g, ss, k);
+    }
+}
+
 void case_stripes() {
     const Csr g = rmat(8, 10, 8);
     std::vector<Sched> ss = motif_schedules(g, 4, true, 1);
@@ -416,13 +442,14 @@ void case_stripes() {
 int main(int argc, char** argv) {
     std::vector<std::string> cases;
     for (int i = 1; i < argc; ++i) cases.push_back(argv[i]);
-    if (cases.empty()) cases = {"quick", "pair", "pairhub", "stripes", "vec"};
+    if (cases.empty()) cases = {"quick", "pair", "pairhub", "pairtags", "stripes", "vec"};
     for (const std::string& c : cases) {
         if (c == "quick") case_quick();
         else if (c == "donation") case_donation();
         else if (c == "leafslices") case_leafslices();
         else if (c == "pair") case_pair();
         else if (c == "pairhub") case_pairhub();
+        else if (c == "pairtags") case_pairtags();
         else if (c == "stripes") case_stripes();
         else if (c == "vec") case_vec();
         else {

@@ -53,7 +53,7 @@ def _build() -> Path:
 def test_device_core_on_emulated_warps():
     exe = _build()
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
-    r = subprocess.run([str(exe), "quick", "pair", "pairhub", "stripes", "vec"], capture_output=True, text=True, timeout=900, env=env)
+    r = subprocess.run([str(exe), "quick", "pair", "pairhub", "pairtags", "stripes", "vec"], capture_output=True, text=True, timeout=900, env=env)
     tail = (r.stdout[-3000:] + "\n" + r.stderr[-3000:]).strip()
     assert r.returncode == 0, tail
     assert "PASSED (0 mismatches)" in r.stdout, tail
