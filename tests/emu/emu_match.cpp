@@ -5,8 +5,9 @@
 // every set slot is followed by a poisoned guard, so a set written past its
 // slot or a warp past its region is reported at the faulting access.
 //
-//   emu_match [case ...]     cases: quick, donation, pair, stripes
-//                            (default: quick pair stripes)
+//   emu_match [case ...]     cases: quick, donation, leafslices, pair,
+//                            pairhub, pairtags, stripes, vec, rows
+//                            (default: all but donation and leafslices)
 #include <sanitizer/asan_interface.h>
 
 #include <atomic>
@@ -23,6 +24,7 @@
 
 namespace gpm {
 #include "match_core.cuh"
+#include "csr_rows.cuh"
 }
 
 extern "C" int oracle_pattern_matching(int V, const uint32_t* rp, const int32_t* col, const int64_t* tables, int nw,
@@ -401,6 +403,69 @@ void case_pairtags() {
     }
 }
 
+// The upload kernels' row search (csr_rows.cuh) on one emulated warp:
+// chunks of positions as validate_kernel and relabel_fill_kernel take them,
+// on CSRs with long runs of empty rows and with hubs, against each
+// position's true row.
+void case_rows() {
+    unsigned long long state = 88172645463325252ull;
+    auto rnd = [&](unsigned long long m) {
+        state ^= state << 13;
+        state ^= state >> 7;
+        state ^= state << 17;
+        return state % m;
+    };
+    int bad = 0, graphs = 0;
+    for (int trial = 0; trial < 60; ++trial) {
+        const int V = 1 + (int)rnd(2500);
+        std::vector<unsigned> rp(V + 1, 0);
+        for (int v = 0; v < V; ++v) {
+            unsigned d = (unsigned)rnd(6);
+            if (trial % 3 == 0 && rnd(10) < 9) d = 0;   // long runs of empty rows
+            if (trial % 5 == 0 && rnd(500) == 0) d = 200 + (unsigned)rnd(1500);  // hubs
+            rp[v + 1] = rp[v] + d;
+        }
+        const unsigned long long E = rp[V];
+        std::vector<int> truth(E);
+        for (int v = 0; v < V; ++v)
+            for (unsigned k = rp[v]; k < rp[v + 1]; ++k) truth[k] = v;
+        const unsigned long long chunk = trial % 2 ? 4096 : 32 + rnd(200);
+        gpm_emu::block_dim = {32, 1, 1};
+        gpm_emu::grid_dim = {1, 1, 1};
+        std::vector<unsigned char> smem(16);
+        gpm_emu::Warp* w = new gpm_emu::Warp();
+        for (int l = 0; l < 32; ++l) {
+            w->th[l].tid = {(unsigned)l, 0, 0};
+            w->th[l].bid = {0, 0, 0};
+            w->th[l].smem = smem.data();
+        }
+        std::atomic<int> wrong{0};
+        auto body = [&](int) {
+            const int lane = (int)(threadIdx.x & 31);
+            for (unsigned long long c0 = 0; c0 < E; c0 += chunk) {
+                const unsigned long long c1 = std::min(E, c0 + chunk);
+                int r0 = 0;
+                if (lane == 0) r0 = csr_row_of(rp.data(), V, c0);
+                r0 = __shfl_sync(kFull, r0, 0);
+                for (unsigned long long kb = c0; kb < c1; kb += 32) {
+                    const int row = csr_batch_row(rp.data(), V, kb, c1, r0, lane);
+                    const unsigned long long k = kb + (unsigned long long)lane;
+                    if (k < c1 && row != truth[k]) wrong.fetch_add(1);
+                }
+            }
+        };
+        gpm_emu::run_warp(*w, body);
+        delete w;
+        bad += wrong.load();
+        ++graphs;
+    }
+    if (bad) {
+        std::printf("MISMATCH rows: %d positions got the wrong row\n", bad);
+        ++failures;
+    }
+    std::printf("ok rows: %d CSRs\n", graphs);
+}
+
 void case_stripes() {
     const Csr g = rmat(8, 10, 8);
     std::vector<Sched> ss = motif_schedules(g, 4, true, 1);
@@ -443,7 +508,7 @@ void case_stripes() {
 int main(int argc, char** argv) {
     std::vector<std::string> cases;
     for (int i = 1; i < argc; ++i) cases.push_back(argv[i]);
-    if (cases.empty()) cases = {"quick", "pair", "pairhub", "pairtags", "stripes", "vec"};
+    if (cases.empty()) cases = {"quick", "pair", "pairhub", "pairtags", "stripes", "vec", "rows"};
     for (const std::string& c : cases) {
         if (c == "quick") case_quick();
         else if (c == "donation") case_donation();
@@ -451,6 +516,7 @@ int main(int argc, char** argv) {
         else if (c == "pair") case_pair();
         else if (c == "pairhub") case_pairhub();
         else if (c == "pairtags") case_pairtags();
+        else if (c == "rows") case_rows();
         else if (c == "stripes") case_stripes();
         else if (c == "vec") case_vec();
         else {

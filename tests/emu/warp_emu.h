@@ -254,6 +254,9 @@ inline unsigned __ballot_sync(unsigned, int pred, gpm_emu_loc loc = gpm_emu_loc:
         },
         loc);
 }
+inline int __all_sync(unsigned mask, int pred, gpm_emu_loc loc = gpm_emu_loc::current()) {
+    return __ballot_sync(mask, pred, loc) == 0xffffffffu;
+}
 template <class T>
 inline unsigned __match_any_sync(unsigned, T v, gpm_emu_loc loc = gpm_emu_loc::current()) {
     const unsigned long long mine = gpm_emu::to_bits(v);

@@ -10,7 +10,9 @@ grab size and that add up to the whole job (the multi-rank split); any
 out-of-bounds access, any lane that meets a different shuffle/ballot/syncwarp
 than its warp, and any internal check stops the run.  After every launch the
 dense counters and leaf bitmaps must be zero again and every donation slot
-released with no visitor left (the claim protocol's bookkeeping)."""
+released with no visitor left (the claim protocol's bookkeeping).  The
+upload kernels' row search (csr_rows.cuh) runs on one emulated warp over
+CSRs with long runs of empty rows and with hubs."""
 import os
 import shutil
 import subprocess
@@ -53,7 +55,7 @@ def _build() -> Path:
 def test_device_core_on_emulated_warps():
     exe = _build()
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
-    r = subprocess.run([str(exe), "quick", "pair", "pairhub", "pairtags", "stripes", "vec"], capture_output=True, text=True, timeout=900, env=env)
+    r = subprocess.run([str(exe), "quick", "pair", "pairhub", "pairtags", "stripes", "vec", "rows"], capture_output=True, text=True, timeout=900, env=env)
     tail = (r.stdout[-3000:] + "\n" + r.stderr[-3000:]).strip()
     assert r.returncode == 0, tail
     assert "PASSED (0 mismatches)" in r.stdout, tail
