@@ -6,8 +6,8 @@ MLP (gpm_mlp_*: hand-written forward/backward/Adam kernels) predicts the
 log runtime of every candidate instead, trained on runtimes the GPU
 enumerator itself measures; the analytic model remains the fallback (no
 model, or a pattern size the model was not trained for) and measured
-runtime the judge.  Every candidate is an exact schedule, so counts do not
-change with the choice.
+runtime the final arbiter.  Every candidate is an exact schedule, so counts
+do not change with the choice.
 """
 from __future__ import annotations
 
