@@ -51,11 +51,23 @@ def _build() -> Path:
     return exe
 
 
+# the cases, in three groups of similar length run as concurrent processes
+CASE_GROUPS = [["quick", "stripes", "rows"], ["vec", "pair"], ["pairhub", "pairtags"]]
+
+
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
 def test_device_core_on_emulated_warps():
     exe = _build()
     env = dict(os.environ, ASAN_OPTIONS="detect_leaks=0")
-    r = subprocess.run([str(exe), "quick", "pair", "pairhub", "pairtags", "stripes", "vec", "rows"], capture_output=True, text=True, timeout=900, env=env)
-    tail = (r.stdout[-3000:] + "\n" + r.stderr[-3000:]).strip()
-    assert r.returncode == 0, tail
-    assert "PASSED (0 mismatches)" in r.stdout, tail
+    procs = [subprocess.Popen([str(exe), *cases], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env)
+             for cases in CASE_GROUPS]
+    try:
+        outs = [p.communicate(timeout=900) for p in procs]
+    finally:
+        for p in procs:
+            if p.poll() is None:
+                p.kill()
+    for cases, p, (out, err) in zip(CASE_GROUPS, procs, outs):
+        tail = " ".join(cases) + ":\n" + (out[-3000:] + "\n" + err[-3000:]).strip()
+        assert p.returncode == 0, tail
+        assert "PASSED (0 mismatches)" in out, tail
